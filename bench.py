@@ -1,0 +1,343 @@
+"""Benchmark: fp64 Jacobi-PCG time-to-tolerance on the 27-point 160^3
+variable-coefficient diffusion system, one GB300 per rank.
+
+A step is one complete solve from x0 = 0 to ||r|| <= 1e-10 ||b|| (recursive
+residual, the xJPCG stop rule).  The headline metric is solves/s (= 1 /
+time-to-tolerance per GPU, summed over ranks; ranks are independent replicas:
+the path has no data exchange).
+
+  value  inputs resident in HBM: xJPCG_gbSolveDevice on the stored matrix,
+         device-timed with CUDA events on the library's stream.
+  e2e    the reference-facing call xJPCG_cooSolver(MODE_DEFAULT) from pinned
+         host COO arrays: H2D copies, COO->CSR conversion, SpMV tuning, the
+         solve and the D2H copy of x inside the timed region.
+
+``--impl reference`` times the oracle (the C/OpenMP restatement of the
+reference's JPCG; the reference itself only runs on an Alveo U280) on the
+host cores, on bounded samples of iterations of the same system.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"workload": "jpcg_fp64_diffusion27", "grid": "160^3", "n": 4096000, "nnz": 109215352,
+            "stencil": "27-point variable-coefficient diffusion, log-normal(0,1.5) conductances, seed 1",
+            "tol": 1e-10, "max_iter": 20000, "precond": "jacobi", "index": "int32", "dtype": "f64",
+            "l2": "inputs larger than L2 (matrix 1.3 GB)"}
+METRIC = "fp64 JPCG time-to-1e-10 relative residual, 27-pt 160^3 (solves/s = 1/time-to-tol)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=160)
+    ap.add_argument("--cpu-sample-iters", type=int, default=40)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per SpMV launch from the committed ncu summary (or None)."""
+    p = os.path.join(ROOT, "profiles", "spmv_diffusion27_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch_full"), d.get("source", p)
+    return None, None
+
+
+def spmv_bytes(n, nnz):
+    # 12 B per stored entry (f64 value + int32 column), row pointers, x read
+    # once, y written once.
+    return 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
+
+
+def iter_bytes(n, nnz):
+    # SpMV + 11 vector streams of 8 B (update: x, p, r, Ap, J read, x, r
+    # written; p kernel: r, J, p read, p written).
+    return spmv_bytes(n, nnz) + 88 * n
+
+
+def cpu_sample(sysm, iters_full, sample_iters, nthreads=0):
+    """Times `sample_iters` oracle JPCG iterations on the full system."""
+    import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 20000, 1e-10, max_run=sample_iters,
+                nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    per_iter = dt / sample_iters
+    return per_iter, dt
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from hpc_gb300 import workloads as W
+    import oracle
+    oracle.build()
+    sysm = W.diffusion27(args.nx)
+    threads = oracle.max_threads()
+    S = args.cpu_sample_iters
+    # Iterations to tolerance of this system: counted by the oracle itself on
+    # a full solve (untimed), so the sample converts to time-to-tolerance.
+    full = oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 20000, 1e-10)
+    iters = full["k"]
+    for _ in range(args.warmup):
+        cpu_sample(sysm, iters, S)
+    times = [cpu_sample(sysm, iters, S)[0] for _ in range(args.steps)]
+    per_iter = float(np.median(times))
+    ttt = per_iter * iters
+    value = 1.0 / ttt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ttt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(WORKLOAD, parallelism="replicas"),
+            "time_to_tol_s": ttt, "iters": iters,
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": "%d JPCG iterations of the full 160^3 system per step, scaled by the "
+                                       "oracle's own full-solve iteration count (%d)" % (S, iters)},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import ctypes as C
+    import torch
+    import torch.distributed as dist
+
+    import hpc_gb300 as X
+    from hpc_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    sysm = W.diffusion27(args.nx)
+    n, nnz = sysm.n, sysm.nnz
+    rows, cols, vals = sysm.coo()
+    # pinned host copies of the step's inputs for the end-to-end measurement
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    h_rows, h_cols, h_vals = pin(rows), pin(cols), pin(vals)
+    h_diag, h_b = pin(sysm.diag), pin(sysm.b)
+    h_x = torch.zeros(n, dtype=torch.float64).pin_memory()
+    np_ = lambda t: t.numpy()
+
+    h = X.JPCG()
+    stream = torch.cuda.ExternalStream(h.stream())
+    max_iter, tol = WORKLOAD["max_iter"], WORKLOAD["tol"]
+
+    def e2e_step():
+        r = h.coo_solve(n, np_(h_rows), np_(h_cols), np_(h_vals), np_(h_diag), np_(h_b), max_iter, tol,
+                        x=np_(h_x))
+        if r.status != X.SUCCESS:
+            raise RuntimeError(r.message)
+        return r
+
+    r0 = e2e_step()  # sets the matrix, tunes the SpMV
+    info = h.info()
+    d_b = torch.from_numpy(sysm.b).cuda()
+    d_diag = torch.from_numpy(sysm.diag).cuda()
+    d_x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+
+    def solve():
+        st, it, res = h.solve_device(d_b.data_ptr(), d_diag.data_ptr(), d_x.data_ptr(), max_iter, tol)
+        if st != X.SUCCESS:
+            raise RuntimeError(h.last_message())
+        return it
+
+    for _ in range(max(args.warmup, 3)):
+        solve()
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    iters = []
+    ev0.record(stream)
+    for _ in range(args.steps):
+        iters.append(solve())
+        iters[-1] = h.info().itersRun
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    barrier()
+    t = ev0.elapsed_time(ev1) / 1e3
+    t = max_over_ranks(t)
+    ttt = t / args.steps
+    value = world * args.steps / t
+    k_iters = int(np.median(iters))
+    launches = sum(1 + 3 * k for k in iters)
+
+    # Dominant kernel: the SpMV, timed alone on the same stream and matrix.
+    spmv_ms = None
+    reps = 20
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            h.spmv(d_b.data_ptr(), d_x.data_ptr(), on_device=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            h.spmv(d_b.data_ptr(), d_x.data_ptr(), on_device=True)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    spmv_ms = e0.elapsed_time(e1) / reps
+    peak, peak_kind = measured_peak()
+    B = spmv_bytes(n, nnz)
+    achieved = B / (spmv_ms / 1e3) / 1e9
+    traffic, traffic_src = committed_traffic()
+    iter_ms = ttt * 1e3 / max(k_iters, 1)
+    iter_gbs = iter_bytes(n, nnz) / (iter_ms / 1e3) / 1e9
+
+    # End to end through the reference-facing COO call with host buffers.
+    e2e = None
+    if not args.no_e2e:
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        te = max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": world * args.steps / te, "unit": "solves/s",
+               "h2d_bytes_per_step": int(4 * nnz + 4 * nnz + 8 * nnz + 8 * n + 8 * n),
+               "d2h_bytes_per_step": int(8 * n + 256), "time_to_tol_s": te / args.steps,
+               "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle
+        S = args.cpu_sample_iters
+        per_iter, dt = cpu_sample(sysm, k_iters, S)
+        cpu = {"value": 1.0 / (per_iter * k_iters), "unit": "solves/s", "cores": oracle.max_threads(),
+               "kind": "port",
+               "sample": "%d oracle JPCG iterations on the full 160^3 system (%.1f s), scaled to the %d "
+                         "iterations of the GPU solve" % (S, dt, k_iters)}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ttt * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single",
+                               spmv_lanes=info.spmvLanes, spmv_grid=info.spmvGrid),
+                "time_to_tol_s": ttt, "iters": k_iters, "iter_ms": iter_ms, "iter_gbs": iter_gbs,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic,
+                             "kernel": "spmv_staged_kernel (fp64 CSR SpMV)",
+                             "bytes_per_launch": B, "launch_ms": spmv_ms,
+                             "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                             "traffic_source": traffic_src},
+                "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clock_info,
+                "loop": "conditional-graph" if h.info().loopMode == 1 else "host"}
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,260 @@
+"""hpc_gb300 -- GB300-native xJPCG (Jacobi-preconditioned CG with an fp64 CSR SpMV).
+
+The product is ``libXilinxPcg.so`` (C ABI in ``include/pcg.h`` and
+``include/xjpcg_gb300.h``).  This module loads it with ctypes and mirrors the
+reference's xJPCG API (Xilinx/HPC pcg/sw/include/pcg.h) for Python callers and
+tests: the same entry points, argument meaning, status codes and messages.
+
+There is no CPU fallback: if the CUDA library is missing or cannot be loaded,
+``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libXilinxPcg.so")
+
+# XJPCG_Status_t (pcg.h:41-49)
+SUCCESS, NOT_INITIALIZED, ALLOC_FAILED, INVALID_VALUE, EXECUTION_FAILED, INTERNAL_ERROR, \
+    DYNAMIC_LOADING_ERROR = range(7)
+STATUS_NAMES = ["XJPCG_STATUS_SUCCESS", "XJPCG_STATUS_NOT_INITIALIZED", "XJPCG_STATUS_ALLOC_FAILED",
+                "XJPCG_STATUS_INVALID_VALUE", "XJPCG_STATUS_EXECUTION_FAILED", "XJPCG_STATUS_INTERNAL_ERROR",
+                "XJPCG_STATUS_DYNAMIC_LOADING_ERROR"]
+# XJPCG_Mode_t (pcg.h:79-85)
+MODE_DEFAULT, MODE_KEEP_NZ_LAYOUT, MODE_KEEP_MATRIX = 0x00, 0x01, 0x02
+MODE_C_INDEX, MODE_FORTRAN_INDEX = 0x00, 0x10
+
+# Symbols declared in include/pcg.h and include/xjpcg_gb300.h.
+EXPORTED_SYMBOLS = [
+    "xJPCG_getErrorString", "xJPCG_createHandle", "xJPCG_destroyHandle", "xJPCG_cscSymSolver",
+    "xJPCG_cooSolver", "xJPCG_peekAtLastStatus", "xJPCG_getLastMessage", "xJPCG_getMetrics",
+    "xJPCG_gbCsrSolver", "xJPCG_gbSolveDevice", "xJPCG_gbMixedSolve", "xJPCG_gbSpmv", "xJPCG_gbGetCsr",
+    "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes",
+]
+
+
+class Metric(C.Structure):
+    """XJPCG_Metric_t (pcg.h:62-67)."""
+    _fields_ = [("m_objInit", C.c_double), ("m_matProc", C.c_double), ("m_vecProc", C.c_double),
+                ("m_solver", C.c_double)]
+
+
+class GbInfo(C.Structure):
+    """XJPCG_GbInfo_t (xjpcg_gb300.h)."""
+    _fields_ = [("n", C.c_uint32), ("n4", C.c_uint32), ("nnz", C.c_uint64), ("itersRun", C.c_uint32),
+                ("spmvLanes", C.c_uint32), ("spmvGrid", C.c_uint32), ("statusBits", C.c_uint32),
+                ("outerSweeps", C.c_uint32), ("innerIters", C.c_uint32), ("bb", C.c_double),
+                ("rrLast", C.c_double), ("solveMs", C.c_double), ("loopMode", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+RECORD_DTYPE = np.dtype([("id", "<u4"), ("iter", "<u4"), ("vecSize", "<u4"), ("maxIter", "<u4"),
+                         ("tols", "<f8"), ("res", "<f8"), ("rz", "<f8"), ("alpha", "<f8"), ("beta", "<f8"),
+                         ("clock", "<u8")])
+assert RECORD_DTYPE.itemsize == 64
+
+_lib = None
+_P = C.c_void_p
+
+
+def _ptr(a) -> Optional[int]:
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    return a.ctypes.data
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Loads libXilinxPcg.so and declares its signatures.  Raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libXilinxPcg.so is not built (run __graft_entry__.build()); no CPU fallback exists")
+    lib = C.CDLL(path)
+    u32, i64, u64, dbl = C.c_uint32, C.c_int64, C.c_uint64, C.c_double
+    lib.xJPCG_getErrorString.restype = C.c_char_p
+    lib.xJPCG_getErrorString.argtypes = [C.c_int]
+    lib.xJPCG_createHandle.argtypes = [C.POINTER(_P), C.c_char_p]
+    lib.xJPCG_destroyHandle.argtypes = [_P]
+    lib.xJPCG_cscSymSolver.argtypes = [_P, i64, i64, _P, _P, _P, _P, _P, _P, i64, dbl, C.POINTER(i64),
+                                       C.POINTER(dbl), C.c_int]
+    lib.xJPCG_cooSolver.argtypes = [_P, u32, u32, _P, _P, _P, _P, _P, _P, u32, dbl, C.POINTER(u32), C.POINTER(dbl),
+                                    C.c_int]
+    lib.xJPCG_peekAtLastStatus.argtypes = [_P]
+    lib.xJPCG_getLastMessage.restype = C.c_char_p
+    lib.xJPCG_getLastMessage.argtypes = [_P]
+    lib.xJPCG_getMetrics.argtypes = [_P, C.POINTER(Metric)]
+    lib.xJPCG_gbCsrSolver.argtypes = [_P, u32, u32, _P, _P, _P, _P, _P, _P, u32, dbl, C.POINTER(u32),
+                                      C.POINTER(dbl), C.c_int]
+    lib.xJPCG_gbSolveDevice.argtypes = [_P, _P, _P, _P, u32, dbl, C.POINTER(u32), C.POINTER(dbl)]
+    lib.xJPCG_gbMixedSolve.argtypes = [_P, _P, _P, _P, u32, dbl, C.POINTER(u32), C.POINTER(dbl), C.c_int]
+    lib.xJPCG_gbSpmv.argtypes = [_P, _P, _P, C.c_int]
+    lib.xJPCG_gbGetCsr.argtypes = [_P, _P, _P, _P, _P]
+    lib.xJPCG_gbGetRecords.argtypes = [_P, _P, u64, C.POINTER(u64)]
+    lib.xJPCG_gbGetInfo.argtypes = [_P, C.POINTER(GbInfo)]
+    lib.xJPCG_gbGetStream.argtypes = [_P, C.POINTER(_P)]
+    lib.xJPCG_gbSetSpmvLanes.argtypes = [_P, C.c_int]
+    for name in EXPORTED_SYMBOLS:
+        fn = getattr(lib, name)
+        if name not in ("xJPCG_getErrorString", "xJPCG_getLastMessage"):
+            fn.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def error_string(code: int) -> str:
+    return load().xJPCG_getErrorString(code).decode()
+
+
+class XJPCGError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__("%s: %s" % (STATUS_NAMES[status] if 0 <= status < 7 else status, message))
+        self.status = status
+        self.message = message
+
+
+@dataclass
+class SolveResult:
+    status: int
+    x: np.ndarray
+    iters: int
+    res: float
+    message: str
+
+
+class JPCG:
+    """One xJPCG handle (xJPCG_createHandle / xJPCG_destroyHandle).
+
+    Methods mirror the reference's C API; each returns the XJPCG status and the
+    outputs, and never raises for a solver status (check ``.status``).
+    """
+
+    def __init__(self, xclbin: str = ""):
+        self.lib = load()
+        self.h = _P()
+        st = self.lib.xJPCG_createHandle(C.byref(self.h), xclbin.encode())
+        if st != SUCCESS:
+            msg = self.last_message()
+            raise XJPCGError(st, msg)
+
+    def close(self):
+        if self.h:
+            self.lib.xJPCG_destroyHandle(self.h)
+            self.h = _P()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- status ---
+    def last_status(self) -> int:
+        return self.lib.xJPCG_peekAtLastStatus(self.h)
+
+    def last_message(self) -> str:
+        return self.lib.xJPCG_getLastMessage(self.h).decode()
+
+    def metrics(self) -> Metric:
+        m = Metric()
+        self.lib.xJPCG_getMetrics(self.h, C.byref(m))
+        return m
+
+    def info(self) -> GbInfo:
+        i = GbInfo()
+        self.lib.xJPCG_gbGetInfo(self.h, C.byref(i))
+        return i
+
+    def stream(self) -> int:
+        s = _P()
+        self.lib.xJPCG_gbGetStream(self.h, C.byref(s))
+        return s.value or 0
+
+    # --- solvers (pcg.h) ---
+    def coo_solve(self, n, row, col, data, diag, b, max_iter, tol, mode=MODE_DEFAULT, nnz=None,
+                  x: Optional[np.ndarray] = None) -> SolveResult:
+        x = np.zeros(n, np.float64) if x is None else x
+        it, res = C.c_uint32(0), C.c_double(0.0)
+        nnz = len(data) if nnz is None else nnz
+        st = self.lib.xJPCG_cooSolver(self.h, n, nnz, _ptr(row), _ptr(col), _ptr(data), _ptr(diag), _ptr(b), _ptr(x),
+                                      max_iter, tol, C.byref(it), C.byref(res), mode)
+        return SolveResult(st, x, it.value, res.value, self.last_message())
+
+    def csc_sym_solve(self, n, row_idx, col_ptr, data, diag, b, max_iter, tol, mode=MODE_DEFAULT, nnz=None,
+                      x: Optional[np.ndarray] = None) -> SolveResult:
+        x = np.zeros(n, np.float64) if x is None else x
+        it, res = C.c_int64(0), C.c_double(0.0)
+        nnz = len(data) if nnz is None else nnz
+        st = self.lib.xJPCG_cscSymSolver(self.h, n, nnz, _ptr(row_idx), _ptr(col_ptr), _ptr(data), _ptr(diag),
+                                         _ptr(b), _ptr(x), max_iter, tol, C.byref(it), C.byref(res), mode)
+        return SolveResult(st, x, it.value, res.value, self.last_message())
+
+    # --- extensions (xjpcg_gb300.h) ---
+    def csr_solve(self, n, rowptr, col, data, diag, b, max_iter, tol, mode=MODE_DEFAULT,
+                  x: Optional[np.ndarray] = None) -> SolveResult:
+        x = np.zeros(n, np.float64) if x is None else x
+        it, res = C.c_uint32(0), C.c_double(0.0)
+        nnz = len(data)
+        st = self.lib.xJPCG_gbCsrSolver(self.h, n, nnz, _ptr(rowptr), _ptr(col), _ptr(data), _ptr(diag), _ptr(b),
+                                        _ptr(x), max_iter, tol, C.byref(it), C.byref(res), mode)
+        return SolveResult(st, x, it.value, res.value, self.last_message())
+
+    def solve_device(self, d_b: int, d_diag: int, d_x: int, max_iter: int, tol: float):
+        it, res = C.c_uint32(0), C.c_double(0.0)
+        st = self.lib.xJPCG_gbSolveDevice(self.h, d_b, d_diag, d_x, max_iter, tol, C.byref(it), C.byref(res))
+        return st, it.value, res.value
+
+    def mixed_solve(self, b, diag, max_iter, tol, x=None, on_device=False):
+        if not on_device:
+            x = np.zeros(len(b), np.float64) if x is None else x
+        it, res = C.c_uint32(0), C.c_double(0.0)
+        st = self.lib.xJPCG_gbMixedSolve(self.h, _ptr(b), _ptr(diag), _ptr(x), max_iter, tol, C.byref(it),
+                                         C.byref(res), 1 if on_device else 0)
+        return SolveResult(st, x, it.value, res.value, self.last_message())
+
+    def spmv(self, x, y=None, on_device=False):
+        if not on_device and y is None:
+            y = np.zeros(len(x), np.float64)
+        st = self.lib.xJPCG_gbSpmv(self.h, _ptr(x), _ptr(y), 1 if on_device else 0)
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        return y
+
+    def get_csr(self):
+        inf = self.info()
+        n, nnz = inf.n, inf.nnz
+        rp = np.zeros(n + 1, np.int32)
+        ci = np.zeros(nnz, np.int32)
+        v = np.zeros(nnz, np.float64)
+        perm = np.zeros(nnz, np.uint32)
+        st = self.lib.xJPCG_gbGetCsr(self.h, _ptr(rp), _ptr(ci), _ptr(v), _ptr(perm))
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        return rp, ci, v, perm
+
+    def records(self, cap: int = 1 << 20) -> np.ndarray:
+        buf = np.zeros(cap, RECORD_DTYPE)
+        cnt = C.c_uint64(0)
+        st = self.lib.xJPCG_gbGetRecords(self.h, _ptr(buf), cap, C.byref(cnt))
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        return buf[:cnt.value]
+
+    def set_spmv_lanes(self, lanes: int):
+        st = self.lib.xJPCG_gbSetSpmvLanes(self.h, lanes)
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())

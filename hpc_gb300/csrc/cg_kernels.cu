@@ -1,0 +1,193 @@
+// cg_kernels.cu -- the vector kernels of the fp64 Jacobi-PCG iteration.
+//
+// Per iteration the loop runs three launches (captured once in a CUDA graph,
+// inside a conditional WHILE node):
+//   1. SpMV + p.Ap + alpha            (spmv_kernels.cu, mode kCgDot)
+//   2. cg_update_kernel: x += alpha p, r -= alpha Ap, z = J r (not stored),
+//      r.r and r.z reduced over the grid; the last CTA forms beta, writes the
+//      64-byte iteration record, applies the stop rule and sets the loop's
+//      condition.  This fuses the reference's krnl_update_xk (L1/hpc/include/
+//      hw/cgSolver/update_xk.hpp:26-67), krnl_update_rk_jacobi
+//      (update_rk_jacobi.hpp:29-110) and krnl_control (pcg/hw/include/
+//      control.hpp:65-92, tasks.hpp:43-47).
+//   3. cg_pupdate_kernel: p = z + beta p with z = J r recomputed
+//      (update_pk.hpp:26-72).
+// The vector init kernel restates GenCgVector::init (pcg/sw/include/impl/
+// cgVector.hpp:101-114) and the instruction slot 0 (cgVector.hpp:149-159).
+// Reductions are fixed-order (per-CTA tree, then the last CTA sums the CTA
+// partials in index order), so a solve is bitwise reproducible.
+#include "xjpcg_device.cuh"
+#include "xjpcg_internal.hpp"
+
+namespace xjpcg {
+
+constexpr int kVecThreads = 256;
+
+__device__ __forceinline__ void write_record(CgState* s, uint32_t k, double rr, double rz, double alpha,
+                                             double beta) {
+    if (s->records == nullptr || s->recCap < 2) return;
+    const uint32_t slot = (k + 1u < s->recCap) ? k + 1u : 1u + (k % (s->recCap - 1u));
+    IterRecord rec;
+    rec.id = 0;
+    rec.iter = k;
+    rec.vecSize = s->vecSize;
+    rec.maxIter = s->maxIterP1;
+    rec.tols = s->tols;
+    rec.res = rr;
+    rec.rz = rz;
+    rec.alpha = alpha;
+    rec.beta = beta;
+    rec.clock = globaltimer_ns();
+    s->records[slot] = rec;
+}
+
+__global__ void __launch_bounds__(kVecThreads) cg_init_kernel(int n, int n4, const double* __restrict__ b,
+                                                              const double* __restrict__ diag, double* __restrict__ x,
+                                                              double* __restrict__ r, double* __restrict__ p,
+                                                              double* __restrict__ J, double* __restrict__ Ap,
+                                                              CgState* state, double* partials) {
+    double bb = 0.0, rz = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+        const double bi = i < n ? b[i] : 0.0;
+        const double di = i < n ? diag[i] : 1.0;
+        const double ji = 1.0 / di;
+        const double zi = ji * bi;
+        r[i] = bi;
+        J[i] = ji;
+        p[i] = zi;
+        x[i] = 0.0;
+        Ap[i] = 0.0;
+        bb = fma(bi, bi, bb);
+        rz = fma(bi, zi, rz);
+    }
+    double v[2] = {bb, rz};
+    block_sum<kVecThreads, 2, double>(v);
+    double fin[2];
+    if (grid_sum_last<2>(v, partials, &state->counters[1], fin) && threadIdx.x == 0) {
+        CgState* s = state;
+        s->bb = fin[0];
+        s->rz = fin[1];
+        s->rr = fin[0];
+        s->tols = fin[0] * s->tol * s->tol;
+        s->k = 0;
+        s->done = 0;
+        s->status &= ~(kStatusBreakdown | kStatusWaitTimeout);
+        s->vecSize = (uint32_t)n4;
+        if (s->records && s->recCap > 0) {
+            IterRecord rec = {};
+            rec.maxIter = s->maxIterP1;
+            rec.vecSize = (uint32_t)n4;
+            rec.tols = s->tols;
+            rec.res = fin[0];
+            rec.rz = fin[1];
+            rec.clock = globaltimer_ns();
+            s->records[0] = rec;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kVecThreads) cg_update_kernel(int n4, double* __restrict__ x, double* __restrict__ r,
+                                                                const double* __restrict__ p,
+                                                                const double* __restrict__ Ap,
+                                                                const double* __restrict__ J, CgState* state,
+                                                                double* partials) {
+    if (*(volatile uint32_t*)&state->done) {
+        // Only reachable when an earlier kernel of this iteration gave up
+        // (wait timeout); close the loop so the graph cannot spin.
+        if (blockIdx.x == 0 && threadIdx.x == 0 && state->useCond)
+            cudaGraphSetConditional((cudaGraphConditionalHandle)state->condHandle, 0u);
+        return;
+    }
+    const double alpha = state->alpha;
+    double rr = 0.0, rz = 0.0;
+    const int n2 = n4 >> 1;
+    double2* x2 = reinterpret_cast<double2*>(x);
+    double2* r2 = reinterpret_cast<double2*>(r);
+    const double2* p2 = reinterpret_cast<const double2*>(p);
+    const double2* a2 = reinterpret_cast<const double2*>(Ap);
+    const double2* j2 = reinterpret_cast<const double2*>(J);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        double2 xv = x2[i], rv = r2[i];
+        const double2 pv = p2[i], av = __ldcs(&a2[i]), jv = j2[i];
+        xv.x = fma(alpha, pv.x, xv.x);
+        xv.y = fma(alpha, pv.y, xv.y);
+        rv.x = fma(-alpha, av.x, rv.x);
+        rv.y = fma(-alpha, av.y, rv.y);
+        const double z0 = rv.x * jv.x, z1 = rv.y * jv.y;
+        rr = fma(rv.x, rv.x, rr);
+        rr = fma(rv.y, rv.y, rr);
+        rz = fma(rv.x, z0, rz);
+        rz = fma(rv.y, z1, rz);
+        x2[i] = xv;
+        r2[i] = rv;
+    }
+    double v[2] = {rr, rz};
+    block_sum<kVecThreads, 2, double>(v);
+    double fin[2];
+    if (grid_sum_last<2>(v, partials, &state->counters[2], fin) && threadIdx.x == 0) {
+        CgState* s = state;
+        const double rrN = fin[0], rzN = fin[1];
+        const double beta = rzN / s->rz;
+        s->rr = rrN;
+        s->rz = rzN;
+        s->beta = beta;
+        uint32_t k = s->k;
+        write_record(s, k, rrN, rzN, alpha, beta);
+        bool cont = !(rrN < s->tols);
+        ++k;
+        cont = cont && (k < s->maxIterP1);
+        if (!isfinite(alpha) || !isfinite(beta) || !isfinite(rrN)) {
+            s->status |= kStatusBreakdown;
+            cont = false;
+        }
+        if (s->status & kStatusWaitTimeout) cont = false;
+        s->k = k;
+        s->done = cont ? 0u : 1u;
+        if (s->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)s->condHandle, cont ? 1u : 0u);
+    }
+}
+
+__global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double* __restrict__ p,
+                                                                 const double* __restrict__ r,
+                                                                 const double* __restrict__ J, CgState* state) {
+    if (*(volatile uint32_t*)&state->done) return;
+    const double beta = state->beta;
+    const int n2 = n4 >> 1;
+    double2* p2 = reinterpret_cast<double2*>(p);
+    const double2* r2 = reinterpret_cast<const double2*>(r);
+    const double2* j2 = reinterpret_cast<const double2*>(J);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        double2 pv = p2[i];
+        const double2 rv = r2[i], jv = j2[i];
+        pv.x = fma(beta, pv.x, rv.x * jv.x);
+        pv.y = fma(beta, pv.y, rv.y * jv.y);
+        p2[i] = pv;
+    }
+}
+
+int vec_grid(int n4, int numSms) {
+    int need = (n4 / 2 + kVecThreads - 1) / kVecThreads;
+    int cap = numSms * 8;
+    if (need < 1) need = 1;
+    return need < cap ? need : cap;
+}
+
+cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x,
+                           double* r, double* p, double* J, double* Ap, CgState* state, double* partials) {
+    cg_init_kernel<<<grid, kVecThreads, 0, st>>>(n, n4, b, diag, x, r, p, J, Ap, state, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* x, double* r, const double* p,
+                             const double* Ap, const double* J, CgState* state, double* partials) {
+    cg_update_kernel<<<grid, kVecThreads, 0, st>>>(n4, x, r, p, Ap, J, state, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* p, const double* r, const double* J,
+                              CgState* state) {
+    cg_pupdate_kernel<<<grid, kVecThreads, 0, st>>>(n4, p, r, J, state);
+    return cudaGetLastError();
+}
+
+}  // namespace xjpcg

@@ -1,0 +1,345 @@
+// pcg_api.cpp -- the extern "C" boundary of libXilinxPcg.so.
+//
+// The pcg.h entry points follow pcg/sw/src/pcg.cpp:34-215 step for step: mode
+// dispatch on (mode & 0x0f), index base (mode & 0xf0) >> 4, first-call check
+// for the reuse modes, the four metric phases, res = sqrt(Res / bb), and
+// EXECUTION_FAILED when res > tol with x, iter and res still written.  No C++
+// exception crosses this boundary.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "pcg_handle.hpp"
+
+using xjpcg::CgError;
+using xjpcg::PcgHandle;
+
+namespace {
+
+double elapsed(std::chrono::time_point<std::chrono::high_resolution_clock>& last) {
+    auto now = std::chrono::high_resolution_clock::now();
+    std::chrono::duration<double> d = now - last;
+    last = now;
+    return d.count();
+}
+
+PcgHandle* impl(XJPCG_Handle_t* h) { return reinterpret_cast<PcgHandle*>(h); }
+const PcgHandle* impl(const XJPCG_Handle_t* h) { return reinterpret_cast<const PcgHandle*>(h); }
+
+// The index base of a mode; the reference rejects anything but 0 and 1 in
+// SparseMatrix::loadCoo / loadCscSym (matrix_params.hpp:51-60, 82-96) with an
+// SpmNotSupported exception that surfaces as INTERNAL_ERROR.
+int modeBase(int mode) {
+    const int base = (mode & 0xf0) >> 4;
+    if (base != 0 && base != 1)
+        throw xjpcg::InternalError("from getCooDatFromCscSym in gen_signature.hpp, unsupported storage mode.");
+    return base;
+}
+
+void finishSolve(PcgHandle* p, const xjpcg::Results& r, double tol, double* res, uint32_t* iter32, int64_t* iter64,
+                 std::chrono::time_point<std::chrono::high_resolution_clock>& last) {
+    *res = std::sqrt(r.rrLast / r.bb);
+    if (iter32) *iter32 = r.reportedIters;
+    if (iter64) *iter64 = r.reportedIters;
+    p->markCalled();
+    p->metrics()->m_solver = elapsed(last);
+    if (r.status & xjpcg::kStatusBreakdown)
+        throw xjpcg::ExecFailed("breakdown (non-finite alpha, beta or r.r) after " + std::to_string(r.reportedIters) +
+                                " iterations.");
+    if (*res > tol)
+        throw xjpcg::ExecFailed("exit with divergent solution after " + std::to_string(r.reportedIters) +
+                                " iterations.");
+}
+
+}  // namespace
+
+extern "C" {
+
+XJPCG_Status_t xJPCG_createHandle(XJPCG_Handle_t** handle, const char* xclbinPath) {
+    (void)xclbinPath;
+    if (handle == nullptr) return XJPCG_STATUS_INVALID_VALUE;
+    PcgHandle* p = new (std::nothrow) PcgHandle();
+    if (p == nullptr) return XJPCG_STATUS_ALLOC_FAILED;
+    *handle = reinterpret_cast<XJPCG_Handle_t*>(p);
+    try {
+        auto last = std::chrono::high_resolution_clock::now();
+        p->init();
+        p->metrics()->m_objInit = elapsed(last);
+    } catch (const CgError& e) {
+        return p->setStatusMessage(e.status, e.what());
+    } catch (const std::exception& e) {
+        return p->setStatusMessage(XJPCG_STATUS_INTERNAL_ERROR, e.what());
+    }
+    return p->setStatusMessage(XJPCG_STATUS_SUCCESS, "Handle is created successfully");
+}
+
+XJPCG_Status_t xJPCG_destroyHandle(XJPCG_Handle_t* handle) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    delete impl(handle);
+    return XJPCG_STATUS_SUCCESS;
+}
+
+XJPCG_Status_t xJPCG_cscSymSolver(XJPCG_Handle_t* handle, const int64_t p_n, const int64_t p_nnz,
+                                  const int64_t* p_rowIdx, const int64_t* p_colPtr, const double* p_data,
+                                  const double* p_diagA, const double* p_b, const double* p_x,
+                                  const int64_t p_maxIter, const double p_tol, int64_t* p_iter, double* p_res,
+                                  const XJPCG_Mode_t mode) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    PcgHandle* p = impl(handle);
+    try {
+        auto last = std::chrono::high_resolution_clock::now();
+        const bool first = p->isFirstCall();
+        // PCGImpl::setCscSymMat / updateCscSymMat argument checks
+        // (pcgImp.hpp:78-86, 124-132); the narrowing to uint32_t is the
+        // reference's own (pcgImp.hpp:72-77).
+        const uint32_t n = (uint32_t)p_n;
+        const uint32_t nnz = (uint32_t)p_nnz;
+        switch (mode & 0x0f) {
+            case XJPCG_MODE_DEFAULT: {
+                if (n == 0) throw xjpcg::InvalidValue("Wrong dimension size.");
+                if (nnz == 0) throw xjpcg::InvalidValue("Wrong non-zero element size.");
+                if (p_rowIdx == nullptr || p_colPtr == nullptr || p_data == nullptr)
+                    throw xjpcg::InvalidValue("Matrix is nullptr.");
+                p->setCscSymMat(n, nnz, p_rowIdx, p_colPtr, p_data, modeBase(mode));
+                break;
+            }
+            case XJPCG_MODE_KEEP_NZ_LAYOUT: {
+                if (first)
+                    throw xjpcg::InvalidValue("wrong solver mode for the first call, please use XJPCG_MODEL_DEFAULT.");
+                if (n == 0) throw xjpcg::InvalidValue("Wrong dimension size.");
+                if (nnz == 0) throw xjpcg::InvalidValue("Wrong non-zero element size.");
+                if (p_data == nullptr) throw xjpcg::InvalidValue("Matrix is nullptr.");
+                p->updateCscSymValues(n, nnz, p_rowIdx, p_colPtr, p_data, modeBase(mode));
+                break;
+            }
+            default:
+                if (first)
+                    throw xjpcg::InvalidValue("wrong solver mode for the first call, please use XJPCG_MODEL_DEFAULT.");
+                break;
+        }
+        p->metrics()->m_matProc = elapsed(last);
+        if (p_maxIter < 0) throw xjpcg::InvalidValue("negative maximum iteration count.");
+        p->setVec(n, p_b, p_diagA, false);
+        p->metrics()->m_vecProc = elapsed(last);
+        xjpcg::Results r = p->run((uint32_t)p_maxIter, p_tol);
+        p->copyX(const_cast<double*>(p_x), n, false);
+        finishSolve(p, r, p_tol, p_res, nullptr, p_iter, last);
+    } catch (const CgError& e) {
+        return p->setStatusMessage(e.status, e.what());
+    } catch (const std::exception& e) {
+        return p->setStatusMessage(XJPCG_STATUS_INTERNAL_ERROR, e.what());
+    }
+    return p->setStatusMessage(XJPCG_STATUS_SUCCESS, "Solver returns successfully");
+}
+
+XJPCG_Status_t xJPCG_cooSolver(XJPCG_Handle_t* handle, const uint32_t p_n, const uint32_t p_nnz,
+                               const uint32_t* p_rowIdx, const uint32_t* p_colIdx, const double* p_data,
+                               const double* matJ, const double* b, const double* x, const uint32_t p_maxIter,
+                               const double p_tol, uint32_t* p_iter, double* p_res, const XJPCG_Mode_t mode) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    PcgHandle* p = impl(handle);
+    try {
+        auto last = std::chrono::high_resolution_clock::now();
+        const bool first = p->isFirstCall();
+        switch (mode & 0x0f) {
+            case XJPCG_MODE_DEFAULT:
+                // PCGImpl::setCooMat checks (pcgImp.hpp:55-63)
+                if (p_n == 0) throw xjpcg::InvalidValue("Wrong dimension size.");
+                if (p_nnz == 0) throw xjpcg::InvalidValue("Wrong non-zero element size.");
+                if (p_rowIdx == nullptr || p_colIdx == nullptr || p_data == nullptr)
+                    throw xjpcg::InvalidValue("Matrix is nullptr.");
+                p->setCooMat(p_n, p_nnz, p_rowIdx, p_colIdx, p_data, modeBase(mode));
+                break;
+            case XJPCG_MODE_KEEP_NZ_LAYOUT:
+                if (first)
+                    throw xjpcg::InvalidValue("wrong solver mode for the first call, please use XJPCG_MODEL_DEFAULT.");
+                // PCGImpl::updateMat checks (pcgImp.hpp:96-104); indices unused
+                if (p_n == 0) throw xjpcg::InvalidValue("Wrong dimension size.");
+                if (p_nnz == 0) throw xjpcg::InvalidValue("Wrong non-zero element size.");
+                if (p_data == nullptr) throw xjpcg::InvalidValue("Matrix is nullptr.");
+                p->updateCooValues(p_n, p_nnz, p_data);
+                break;
+            default:
+                if (first)
+                    throw xjpcg::InvalidValue("wrong solver mode for the first call, please use XJPCG_MODEL_DEFAULT.");
+                break;
+        }
+        p->metrics()->m_matProc = elapsed(last);
+        p->setVec(p_n, b, matJ, false);
+        p->metrics()->m_vecProc = elapsed(last);
+        xjpcg::Results r = p->run(p_maxIter, p_tol);
+        p->copyX(const_cast<double*>(x), p_n, false);
+        finishSolve(p, r, p_tol, p_res, p_iter, nullptr, last);
+    } catch (const CgError& e) {
+        return p->setStatusMessage(e.status, e.what());
+    } catch (const std::exception& e) {
+        return p->setStatusMessage(XJPCG_STATUS_INTERNAL_ERROR, e.what());
+    }
+    return p->setStatusMessage(XJPCG_STATUS_SUCCESS, "Solver returns successfully");
+}
+
+XJPCG_Status_t xJPCG_getMetrics(const XJPCG_Handle_t* handle, XJPCG_Metric_t* metric) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    const PcgHandle* p = impl(handle);
+    if (metric == nullptr) return p->setStatusMessage(XJPCG_STATUS_INVALID_VALUE, "INVALID VALUE ERROR: metric is nullptr.");
+    *metric = *p->metrics();
+    return p->setStatusMessage(XJPCG_STATUS_SUCCESS, "Get metrics successfully");
+}
+
+XJPCG_Status_t xJPCG_peekAtLastStatus(const XJPCG_Handle_t* handle) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    return impl(handle)->lastStatus();
+}
+
+const char* xJPCG_getLastMessage(const XJPCG_Handle_t* handle) {
+    if (handle == nullptr) return "Can't retrieve last error message from a null JPCG handle.";
+    return impl(handle)->lastMessage().c_str();
+}
+
+const char* xJPCG_getErrorString(const XJPCG_Status_t code) {
+    switch (code) {
+        case XJPCG_STATUS_SUCCESS:
+            return "XJPCG_STATUS_SUCCESS";
+        case XJPCG_STATUS_NOT_INITIALIZED:
+            return "XJPCG_STATUS_NOT_INITIALIZED";
+        case XJPCG_STATUS_ALLOC_FAILED:
+            return "XJPCG_STATUS_ALLOC_FAILED";
+        case XJPCG_STATUS_INVALID_VALUE:
+            return "XJPCG_STATUS_INVALID_VALUE";
+        case XJPCG_STATUS_EXECUTION_FAILED:
+            return "XJPCG_STATUS_EXECUTION_FAILED";
+        case XJPCG_STATUS_INTERNAL_ERROR:
+            return "XJPCG_STATUS_INTERNAL_ERROR";
+        case XJPCG_STATUS_DYNAMIC_LOADING_ERROR:
+            return "XJPCG_STATUS_DYNAMIC_LOADING_ERROR";
+    }
+    return "Unknown Error Code!";
+}
+
+// ---------------------------------------------------------------------------
+// Extensions (xjpcg_gb300.h)
+// ---------------------------------------------------------------------------
+#define XJ_GUARD_BEGIN                                 \
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED; \
+    PcgHandle* p = impl(handle);                        \
+    try {
+#define XJ_GUARD_END(msg)                                               \
+    }                                                                   \
+    catch (const CgError& e) {                                          \
+        return p->setStatusMessage(e.status, e.what());                 \
+    }                                                                   \
+    catch (const std::exception& e) {                                   \
+        return p->setStatusMessage(XJPCG_STATUS_INTERNAL_ERROR, e.what()); \
+    }                                                                   \
+    return p->setStatusMessage(XJPCG_STATUS_SUCCESS, msg);
+
+XJPCG_Status_t xJPCG_gbCsrSolver(XJPCG_Handle_t* handle, uint32_t n, uint32_t nnz, const int32_t* rowPtr,
+                                 const int32_t* colIdx, const double* data, const double* diagA, const double* b,
+                                 double* x, uint32_t maxIter, double tol, uint32_t* iter, double* res,
+                                 XJPCG_Mode_t mode) {
+    XJ_GUARD_BEGIN
+    auto last = std::chrono::high_resolution_clock::now();
+    const bool first = p->isFirstCall();
+    switch (mode & 0x0f) {
+        case XJPCG_MODE_DEFAULT:
+            if (n == 0) throw xjpcg::InvalidValue("Wrong dimension size.");
+            if (nnz == 0) throw xjpcg::InvalidValue("Wrong non-zero element size.");
+            if (rowPtr == nullptr || colIdx == nullptr || data == nullptr)
+                throw xjpcg::InvalidValue("Matrix is nullptr.");
+            p->setCsrMat(n, nnz, rowPtr, colIdx, data, modeBase(mode));
+            break;
+        case XJPCG_MODE_KEEP_NZ_LAYOUT:
+            if (first) throw xjpcg::InvalidValue("wrong solver mode for the first call, please use XJPCG_MODEL_DEFAULT.");
+            if (data == nullptr) throw xjpcg::InvalidValue("Matrix is nullptr.");
+            p->updateCsrValues(n, nnz, data);
+            break;
+        default:
+            if (first) throw xjpcg::InvalidValue("wrong solver mode for the first call, please use XJPCG_MODEL_DEFAULT.");
+            break;
+    }
+    p->metrics()->m_matProc = elapsed(last);
+    p->setVec(n, b, diagA, false);
+    p->metrics()->m_vecProc = elapsed(last);
+    xjpcg::Results r = p->run(maxIter, tol);
+    p->copyX(x, n, false);
+    finishSolve(p, r, tol, res, iter, nullptr, last);
+    XJ_GUARD_END("Solver returns successfully")
+}
+
+XJPCG_Status_t xJPCG_gbSolveDevice(XJPCG_Handle_t* handle, const double* d_b, const double* d_diagA, double* d_x,
+                                   uint32_t maxIter, double tol, uint32_t* iter, double* res) {
+    XJ_GUARD_BEGIN
+    auto last = std::chrono::high_resolution_clock::now();
+    if (!p->hasMatrix()) throw xjpcg::InvalidValue("no matrix has been set.");
+    p->metrics()->m_matProc = 0.0;
+    p->setVec(p->matrixN(), d_b, d_diagA, true);
+    p->metrics()->m_vecProc = elapsed(last);
+    xjpcg::Results r = p->run(maxIter, tol);
+    if (d_x) p->copyX(d_x, p->matrixN(), true);
+    finishSolve(p, r, tol, res, iter, nullptr, last);
+    XJ_GUARD_END("Solver returns successfully")
+}
+
+XJPCG_Status_t xJPCG_gbMixedSolve(XJPCG_Handle_t* handle, const double* b, const double* diagA, double* x,
+                                  uint32_t maxIter, double tol, uint32_t* iter, double* res, int onDevice) {
+    XJ_GUARD_BEGIN
+    auto last = std::chrono::high_resolution_clock::now();
+    if (!p->hasMatrix()) throw xjpcg::InvalidValue("no matrix has been set.");
+    p->metrics()->m_matProc = 0.0;
+    p->setVec(p->matrixN(), b, diagA, onDevice != 0);
+    p->metrics()->m_vecProc = elapsed(last);
+    xjpcg::Results r = p->runMixed(maxIter, tol);
+    if (x) p->copyX64(x, p->matrixN(), onDevice != 0);
+    *res = std::sqrt(r.rrLast / r.bb);
+    if (iter) *iter = r.reportedIters;
+    p->metrics()->m_solver = elapsed(last);
+    if (r.status & xjpcg::kStatusBreakdown) throw xjpcg::ExecFailed("breakdown in the refinement loop.");
+    if (!(*res <= tol))
+        throw xjpcg::ExecFailed("exit with divergent solution after " + std::to_string(r.reportedIters) +
+                                " inner iterations.");
+    XJ_GUARD_END("Solver returns successfully")
+}
+
+XJPCG_Status_t xJPCG_gbSpmv(XJPCG_Handle_t* handle, const double* x, double* y, int onDevice) {
+    XJ_GUARD_BEGIN
+    if (x == nullptr || y == nullptr) throw xjpcg::InvalidValue("Vector is nullptr.");
+    p->spmv(x, y, onDevice != 0);
+    XJ_GUARD_END("SpMV returns successfully")
+}
+
+XJPCG_Status_t xJPCG_gbGetCsr(XJPCG_Handle_t* handle, int32_t* rowPtr, int32_t* colIdx, double* values,
+                              uint32_t* perm) {
+    XJ_GUARD_BEGIN
+    p->getCsr(rowPtr, colIdx, values, perm);
+    XJ_GUARD_END("Get CSR successfully")
+}
+
+XJPCG_Status_t xJPCG_gbGetRecords(XJPCG_Handle_t* handle, void* buf, uint64_t cap, uint64_t* count) {
+    XJ_GUARD_BEGIN
+    if (buf == nullptr || count == nullptr) throw xjpcg::InvalidValue("buffer is nullptr.");
+    *count = p->getRecords(buf, cap);
+    XJ_GUARD_END("Get records successfully")
+}
+
+XJPCG_Status_t xJPCG_gbGetInfo(const XJPCG_Handle_t* handle, XJPCG_GbInfo_t* info) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    if (info == nullptr) return XJPCG_STATUS_INVALID_VALUE;
+    impl(handle)->fillInfo(info);
+    return XJPCG_STATUS_SUCCESS;
+}
+
+XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    if (stream == nullptr) return XJPCG_STATUS_INVALID_VALUE;
+    *stream = (void*)impl(handle)->stream();
+    return XJPCG_STATUS_SUCCESS;
+}
+
+XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes) {
+    XJ_GUARD_BEGIN
+    p->setLanes(lanes);
+    XJ_GUARD_END("SpMV lanes set successfully")
+}
+
+}  // extern "C"

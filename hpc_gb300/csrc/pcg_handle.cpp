@@ -1,0 +1,668 @@
+// pcg_handle.cpp -- host orchestration of the GB300 xJPCG solver.
+#include "pcg_handle.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+
+namespace xjpcg {
+
+namespace {
+constexpr uint64_t kMaxRecords = 1ull << 20;  // ring of records beyond this
+constexpr int kPartialSlots = 4 * 8192;       // doubles; >= 2 * max grid
+constexpr int kMaxOuter = 64;
+
+int envInt(const char* name, int dflt) {
+    const char* v = std::getenv(name);
+    return v ? std::atoi(v) : dflt;
+}
+double envDouble(const char* name, double dflt) {
+    const char* v = std::getenv(name);
+    return v ? std::atof(v) : dflt;
+}
+}  // namespace
+
+bool DevBuf::ensure(size_t b, uint64_t* generation) {
+    if (b == 0) b = 16;
+    if (b <= bytes) return true;
+    release();
+    if (cudaMalloc(&p, b) != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+        return false;
+    }
+    bytes = b;
+    if (generation) ++*generation;
+    return true;
+}
+
+PcgHandle::~PcgHandle() {
+    if (m_exec) cudaGraphExecDestroy(m_exec);
+    if (m_mixedExec) cudaGraphExecDestroy(m_mixedExec);
+    if (m_ev0) cudaEventDestroy(m_ev0);
+    if (m_ev1) cudaEventDestroy(m_ev1);
+    if (m_stream) cudaStreamDestroy(m_stream);
+}
+
+void PcgHandle::check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return;
+    cudaGetLastError();
+    if (e == cudaErrorMemoryAllocation) throw AllocFailed(std::string(what) + ": " + cudaGetErrorString(e));
+    throw InternalError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void PcgHandle::alloc(DevBuf& b, size_t bytes, const char* what) {
+    if (!b.ensure(bytes, &m_generation)) throw AllocFailed(std::string("device allocation failed for ") + what);
+}
+
+void PcgHandle::init() {
+    check(cudaGetDevice(&m_device), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&m_numSms, cudaDevAttrMultiProcessorCount, m_device), "cudaDeviceGetAttribute");
+    check(cudaStreamCreateWithFlags(&m_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaEventCreate(&m_ev0), "cudaEventCreate");
+    check(cudaEventCreate(&m_ev1), "cudaEventCreate");
+    alloc(m_state, sizeof(CgState), "solver state");
+    alloc(m_state32, sizeof(CgState), "solver state");
+    alloc(m_partials, sizeof(double) * kPartialSlots, "reduction partials");
+    alloc(m_flags, 8 * sizeof(int), "flags");
+    check(cudaMemsetAsync(m_state.p, 0, sizeof(CgState), m_stream), "memset");
+    check(cudaMemsetAsync(m_state32.p, 0, sizeof(CgState), m_stream), "memset");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    m_useGraph = envInt("XJPCG_HOST_LOOP", 0) == 0;
+    m_forcedLanes = envInt("XJPCG_SPMV_LANES", 0);
+}
+
+// ---------------------------------------------------------------------------
+// Matrix set-up
+// ---------------------------------------------------------------------------
+void PcgHandle::setCooMat(uint32_t n, uint64_t nnz, const uint32_t* row, const uint32_t* col, const double* data,
+                          int base) {
+    if (nnz > 0x7ffffff0ull) throw InvalidValue("number of non-zeros exceeds 2^31 - 16.");
+    m_haveMatrix = false;
+    alloc(m_inRow, sizeof(uint32_t) * nnz, "COO rows");
+    alloc(m_inCol, sizeof(uint32_t) * nnz, "COO cols");
+    alloc(m_inVal, sizeof(double) * nnz, "COO values");
+    check(cudaMemcpyAsync(m_inRow.p, row, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D rows");
+    check(cudaMemcpyAsync(m_inCol.p, col, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D cols");
+    check(cudaMemcpyAsync(m_inVal.p, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D values");
+    const uint64_t nnzPad = (nnz + 3) / 4 * 4 + 4;
+    alloc(m_rowptr, sizeof(int) * ((size_t)n + 1), "CSR row pointers");
+    alloc(m_col, sizeof(int) * nnzPad, "CSR columns");
+    alloc(m_val, sizeof(double) * nnzPad, "CSR values");
+    alloc(m_perm, sizeof(uint32_t) * (nnz + 1), "CSR permutation");
+    alloc(m_counts, sizeof(int) * ((size_t)n + 2), "conversion counts");
+    alloc(m_fill, sizeof(int) * ((size_t)n + 1), "conversion fill");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count((int)std::max<uint64_t>(n + 1, nnz + 1)) + 16),
+          "scan scratch");
+    alloc(m_keys, sizeof(uint64_t) * (nnz + 1), "conversion keys");
+    ConvertScratch s;
+    s.counts = m_counts.as<int>();
+    s.fill = m_fill.as<int>();
+    s.blockSums = m_blockSums.as<int>();
+    s.keys = m_keys.as<uint64_t>();
+    s.flags = m_flags.as<int>();
+    int herr = 0;
+    check(coo_to_csr(m_stream, (int)n, (int64_t)nnz, m_inRow.as<uint32_t>(), m_inCol.as<uint32_t>(), base,
+                     m_rowptr.as<int>(), m_col.as<int>(), m_perm.as<uint32_t>(), s, &herr),
+          "COO to CSR conversion");
+    if (herr & kStatusIndexError) throw InvalidValue("matrix index out of range [base, n + base).");
+    check(gather_values(m_stream, (int64_t)nnz, m_perm.as<uint32_t>(), m_inVal.as<double>(), m_val.as<double>()),
+          "value gather");
+    m_n = n;
+    m_nnz = nnz;
+    m_kind = 1;
+    finishMatrix();
+}
+
+void PcgHandle::updateCooValues(uint32_t n, uint64_t nnz, const double* data) {
+    // Signature::checkUpdateDim (signature.hpp:575-583) raises SpmInvalidValue,
+    // which the reference reports as INTERNAL_ERROR through std::exception.
+    if (!m_haveMatrix || n != m_n || nnz != m_nnz)
+        throw InternalError("Invalid dimension and/or number of nnzs used for updateing matrix.");
+    alloc(m_inVal, sizeof(double) * nnz, "COO values");
+    check(cudaMemcpyAsync(m_inVal.p, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D values");
+    check(gather_values(m_stream, (int64_t)nnz, m_perm.as<uint32_t>(), m_inVal.as<double>(), m_val.as<double>()),
+          "value gather");
+    m_val32Valid = false;
+    check(cudaStreamSynchronize(m_stream), "sync");
+}
+
+void PcgHandle::setCsrMat(uint32_t n, uint64_t nnz, const int32_t* rowPtr, const int32_t* colIdx,
+                          const double* data, int base) {
+    // Row indices are expanded on the host side of the copy: the CSR row
+    // pointer is small (n + 1) and validated here; the rest is the COO path.
+    if ((int64_t)rowPtr[0] - base != 0 || (uint64_t)((int64_t)rowPtr[n] - base) != nnz)
+        throw InvalidValue("CSR row pointer does not span [0, nnz).");
+    std::vector<uint32_t> rows(nnz);
+    for (uint32_t i = 0; i < n; ++i) {
+        const int64_t s = (int64_t)rowPtr[i] - base, e = (int64_t)rowPtr[i + 1] - base;
+        if (e < s) throw InvalidValue("CSR row pointer is not monotone.");
+        for (int64_t k = s; k < e; ++k) rows[k] = i + (uint32_t)base;
+    }
+    setCooMat(n, nnz, rows.data(), reinterpret_cast<const uint32_t*>(colIdx), data, base);
+    m_kind = 3;
+}
+
+void PcgHandle::updateCsrValues(uint32_t n, uint64_t nnz, const double* data) { updateCooValues(n, nnz, data); }
+
+void PcgHandle::setCscSymMat(uint32_t n, uint64_t nnzHalf, const int64_t* rowIdx, const int64_t* colPtr,
+                             const double* data, int base) {
+    // PCGImpl::setCscSymMat: full nnz = 2 * nnz - n (pcgImp.hpp:87).
+    const uint64_t nnzFull = (uint32_t)(nnzHalf * 2 - n);
+    if (base == 1 && colPtr[0] < 1)
+        throw InternalError("from getCooDatFromCscSym in gen_signature.hpp, colPtr[0] start from 1 in FORTRAN storage mode.");
+    if (nnzHalf > 0x7ffffff0ull || nnzFull > 0x7ffffff0ull) throw InvalidValue("number of non-zeros exceeds 2^31 - 16.");
+    alloc(m_inIdx64, sizeof(int64_t) * nnzHalf, "CSC row indices");
+    alloc(m_inPtr64, sizeof(int64_t) * ((size_t)n + 1), "CSC column pointers");
+    alloc(m_cscScratch, sizeof(int) * (nnzHalf + 8), "CSC scratch");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count((int)std::max<uint64_t>(nnzHalf + 1, nnzFull + 1)) + 16),
+          "scan scratch");
+    DevBuf halfVal;
+    if (!halfVal.ensure(sizeof(double) * nnzHalf, nullptr)) throw AllocFailed("device allocation failed for CSC values");
+    check(cudaMemcpyAsync(m_inIdx64.p, rowIdx, sizeof(int64_t) * nnzHalf, cudaMemcpyHostToDevice, m_stream), "H2D");
+    check(cudaMemcpyAsync(m_inPtr64.p, colPtr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, m_stream),
+          "H2D");
+    check(cudaMemcpyAsync(halfVal.p, data, sizeof(double) * nnzHalf, cudaMemcpyHostToDevice, m_stream), "H2D");
+    alloc(m_inRow, sizeof(uint32_t) * nnzFull, "COO rows");
+    alloc(m_inCol, sizeof(uint32_t) * nnzFull, "COO cols");
+    alloc(m_inVal, sizeof(double) * nnzFull, "COO values");
+    int herr = 0;
+    check(cscsym_expand(m_stream, (int)n, (int64_t)nnzHalf, (int64_t)nnzFull, m_inIdx64.as<int64_t>(),
+                        m_inPtr64.as<int64_t>(), halfVal.as<double>(), base, m_inRow.as<uint32_t>(),
+                        m_inCol.as<uint32_t>(), m_inVal.as<double>(), nullptr, m_cscScratch.as<int>(),
+                        m_blockSums.as<int>(), &herr),
+          "symmetric CSC expansion");
+    if (herr & kStatusIndexError) throw InvalidValue("matrix index out of range [base, n + base).");
+    if (herr & kStatusCountError)
+        throw InternalError("from loadCscSym in matrix_params.hpp, failed to convert indices from CscSym to COO format.");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    // The expanded list is a COO input with base 0.
+    std::vector<uint32_t> dummy;
+    const uint64_t nnz = nnzFull;
+    const uint64_t nnzPad = (nnz + 3) / 4 * 4 + 4;
+    alloc(m_rowptr, sizeof(int) * ((size_t)n + 1), "CSR row pointers");
+    alloc(m_col, sizeof(int) * nnzPad, "CSR columns");
+    alloc(m_val, sizeof(double) * nnzPad, "CSR values");
+    alloc(m_perm, sizeof(uint32_t) * (nnz + 1), "CSR permutation");
+    alloc(m_counts, sizeof(int) * ((size_t)n + 2), "conversion counts");
+    alloc(m_fill, sizeof(int) * ((size_t)n + 1), "conversion fill");
+    alloc(m_keys, sizeof(uint64_t) * (nnz + 1), "conversion keys");
+    ConvertScratch s;
+    s.counts = m_counts.as<int>();
+    s.fill = m_fill.as<int>();
+    s.blockSums = m_blockSums.as<int>();
+    s.keys = m_keys.as<uint64_t>();
+    s.flags = m_flags.as<int>();
+    check(coo_to_csr(m_stream, (int)n, (int64_t)nnz, m_inRow.as<uint32_t>(), m_inCol.as<uint32_t>(), 0,
+                     m_rowptr.as<int>(), m_col.as<int>(), m_perm.as<uint32_t>(), s, &herr),
+          "COO to CSR conversion");
+    if (herr & kStatusIndexError) throw InvalidValue("matrix index out of range [base, n + base).");
+    check(gather_values(m_stream, (int64_t)nnz, m_perm.as<uint32_t>(), m_inVal.as<double>(), m_val.as<double>()),
+          "value gather");
+    m_n = n;
+    m_nnz = nnz;
+    m_nnzHalf = nnzHalf;
+    m_kind = 2;
+    finishMatrix();
+}
+
+void PcgHandle::updateCscSymValues(uint32_t n, uint64_t nnzHalf, const int64_t* rowIdx, const int64_t* colPtr,
+                                   const double* data, int base) {
+    const uint64_t nnzFull = (uint32_t)(nnzHalf * 2 - n);
+    if (!m_haveMatrix || n != m_n || nnzFull != m_nnz)
+        throw InternalError("Invalid dimension and/or number of nnzs used for updateing matrix.");
+    if (rowIdx == nullptr || colPtr == nullptr) throw InvalidValue("Matrix is nullptr.");
+    if (base == 1 && colPtr[0] < 1)
+        throw InternalError("from getCooDatFromCscSym in gen_signature.hpp, colPtr[0] start from 1 in FORTRAN storage mode.");
+    alloc(m_inIdx64, sizeof(int64_t) * nnzHalf, "CSC row indices");
+    alloc(m_inPtr64, sizeof(int64_t) * ((size_t)n + 1), "CSC column pointers");
+    alloc(m_cscScratch, sizeof(int) * (nnzHalf + 8), "CSC scratch");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count((int)(nnzHalf + 1)) + 16), "scan scratch");
+    DevBuf halfVal;
+    if (!halfVal.ensure(sizeof(double) * nnzHalf, nullptr)) throw AllocFailed("device allocation failed for CSC values");
+    check(cudaMemcpyAsync(m_inIdx64.p, rowIdx, sizeof(int64_t) * nnzHalf, cudaMemcpyHostToDevice, m_stream), "H2D");
+    check(cudaMemcpyAsync(m_inPtr64.p, colPtr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, m_stream),
+          "H2D");
+    check(cudaMemcpyAsync(halfVal.p, data, sizeof(double) * nnzHalf, cudaMemcpyHostToDevice, m_stream), "H2D");
+    alloc(m_inVal, sizeof(double) * nnzFull, "COO values");
+    int herr = 0;
+    // getCooDatFromCscSym re-expands the values with the new indices
+    // (gen_signature.hpp:73-112); the stored permutation maps them to CSR.
+    check(cscsym_expand(m_stream, (int)n, (int64_t)nnzHalf, (int64_t)nnzFull, m_inIdx64.as<int64_t>(),
+                        m_inPtr64.as<int64_t>(), halfVal.as<double>(), base, nullptr, nullptr, m_inVal.as<double>(),
+                        nullptr, m_cscScratch.as<int>(), m_blockSums.as<int>(), &herr),
+          "symmetric CSC expansion");
+    if (herr & kStatusIndexError) throw InvalidValue("matrix index out of range [base, n + base).");
+    if (herr & kStatusCountError)
+        throw InternalError("from getCooDatFromCscSym in gen_signature.hpp, failed to convert data from CscSym to COO format.");
+    check(gather_values(m_stream, (int64_t)nnzFull, m_perm.as<uint32_t>(), m_inVal.as<double>(), m_val.as<double>()),
+          "value gather");
+    m_val32Valid = false;
+    check(cudaStreamSynchronize(m_stream), "sync");
+}
+
+void PcgHandle::finishMatrix() {
+    // Zero the 4-element alignment pad past nnz (read by the bulk copies).
+    const uint64_t nnzPad = (m_nnz + 3) / 4 * 4 + 4;
+    check(cudaMemsetAsync(m_val.as<double>() + m_nnz, 0, sizeof(double) * (nnzPad - m_nnz), m_stream), "memset");
+    check(cudaMemsetAsync(m_col.as<int>() + m_nnz, 0, sizeof(int) * (nnzPad - m_nnz), m_stream), "memset");
+    m_val32Valid = false;
+    check(cudaStreamSynchronize(m_stream), "sync");
+    m_haveMatrix = true;
+    ensureVectors(m_n);
+    tuneSpmv();
+}
+
+void PcgHandle::setLanes(int lanes) {
+    m_forcedLanes = lanes;
+    if (m_haveMatrix) tuneSpmv();
+}
+
+// Picks the lanes-per-row shape by timing every SpMV configuration on the
+// stored matrix (plain mode, x = p buffer), median of three launches each.
+void PcgHandle::tuneSpmv() {
+    const int ncfg = spmv_num_configs();
+    int best = -1;
+    float bestMs = 1e30f;
+    if (m_forcedLanes > 0) {
+        for (int c = 0; c < ncfg; ++c)
+            if (spmv_config_lanes(c) == m_forcedLanes) best = c;
+        if (best < 0) throw InvalidValue("unsupported SpMV lanes per row.");
+    } else {
+        check(cudaMemsetAsync(m_p.p, 0, sizeof(double) * m_n4, m_stream), "memset");
+        for (int c = 0; c < ncfg; ++c) {
+            const int grid = spmv_grid<double>(c, (int)m_n, m_numSms);
+            if (grid <= 0) continue;
+            float ms[3];
+            for (int rep = 0; rep < 4; ++rep) {
+                check(cudaEventRecord(m_ev0, m_stream), "event");
+                check(spmv_launch<double>(c, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
+                                          m_val.as<double>(), m_p.as<double>(), m_Ap.as<double>(), nullptr,
+                                          m_state.as<CgState>(), m_partials.as<double>(), kSpmvPlain, nullptr),
+                      "SpMV");
+                check(cudaEventRecord(m_ev1, m_stream), "event");
+                check(cudaEventSynchronize(m_ev1), "event");
+                if (rep > 0) check(cudaEventElapsedTime(&ms[rep - 1], m_ev0, m_ev1), "event");
+            }
+            std::sort(ms, ms + 3);
+            if (ms[1] < bestMs) {
+                bestMs = ms[1];
+                best = c;
+            }
+        }
+        if (best < 0) throw InternalError("no SpMV configuration can be launched on this device.");
+    }
+    m_spmvCfg = best;
+    m_spmvGrid = spmv_grid<double>(best, (int)m_n, m_numSms);
+    ++m_generation;  // graphs embed the configuration
+}
+
+// ---------------------------------------------------------------------------
+// Vectors and the solve
+// ---------------------------------------------------------------------------
+void PcgHandle::ensureVectors(uint32_t n) {
+    const uint32_t n4 = (n + 3) / 4 * 4;
+    const size_t vb = sizeof(double) * ((size_t)n4 + 4);
+    alloc(m_b, vb, "b");
+    alloc(m_diag, vb, "diag");
+    alloc(m_x, vb, "x");
+    alloc(m_r, vb, "r");
+    alloc(m_p, vb, "p");
+    alloc(m_J, vb, "J");
+    alloc(m_Ap, vb, "Ap");
+    if (n4 != m_n4) {
+        for (DevBuf* v : {&m_b, &m_diag, &m_x, &m_r, &m_p, &m_J, &m_Ap})
+            check(cudaMemsetAsync(v->p, 0, vb, m_stream), "memset");
+        ++m_generation;
+    }
+    m_vecN = n;
+    m_n4 = n4;
+}
+
+void PcgHandle::setVec(uint32_t n, const double* b, const double* diag, bool onDevice) {
+    // GenCgVector::loadVec / updateVec (cgVector.hpp:55-93).
+    if (b == nullptr || diag == nullptr) throw InvalidValue("Vector is nullptr.");
+    if (!m_haveMatrix || n != m_n) throw InvalidValue("vector dimension differs from the stored matrix.");
+    ensureVectors(n);
+    const cudaMemcpyKind kind = onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    check(cudaMemcpyAsync(m_b.p, b, sizeof(double) * n, kind, m_stream), "copy b");
+    check(cudaMemcpyAsync(m_diag.p, diag, sizeof(double) * n, kind, m_stream), "copy diag");
+    if (!onDevice) check(cudaStreamSynchronize(m_stream), "sync");
+}
+
+void PcgHandle::buildGraph() {
+    if (m_exec && m_execGen == m_generation) return;
+    if (m_exec) {
+        cudaGraphExecDestroy(m_exec);
+        m_exec = nullptr;
+    }
+    const int n = (int)m_n, n4 = (int)m_n4;
+    const int vg = vec_grid(n4, m_numSms);
+    CgState* st = m_state.as<CgState>();
+    double* part = m_partials.as<double>();
+    cudaGraph_t g = nullptr;
+    check(cudaGraphCreate(&g, 0), "cudaGraphCreate");
+    check(cudaStreamBeginCaptureToGraph(m_stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+          "capture");
+    check(cg_init_launch(vg, m_stream, n, n4, m_b.as<double>(), m_diag.as<double>(), m_x.as<double>(),
+                         m_r.as<double>(), m_p.as<double>(), m_J.as<double>(), m_Ap.as<double>(), st, part),
+          "init kernel");
+    check(cudaStreamEndCapture(m_stream, &g), "capture end");
+    size_t numNodes = 0;
+    check(cudaGraphGetNodes(g, nullptr, &numNodes), "graph nodes");
+    std::vector<cudaGraphNode_t> nodes(numNodes);
+    check(cudaGraphGetNodes(g, nodes.data(), &numNodes), "graph nodes");
+    check(cudaGraphConditionalHandleCreate(&m_cond, g, 1, cudaGraphCondAssignDefault), "conditional handle");
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = m_cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t condNode;
+    check(cudaGraphAddNode(&condNode, g, nodes.data(), nullptr, numNodes, &cp), "conditional node");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    check(cudaStreamBeginCaptureToGraph(m_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+          "capture body");
+    check(spmv_launch<double>(m_spmvCfg, m_spmvGrid, m_stream, n, m_rowptr.as<int>(), m_col.as<int>(),
+                              m_val.as<double>(), m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part, kSpmvCgDot,
+                              &st->done),
+          "SpMV kernel");
+    check(cg_update_launch(vg, m_stream, n4, m_x.as<double>(), m_r.as<double>(), m_p.as<double>(),
+                           m_Ap.as<double>(), m_J.as<double>(), st, part),
+          "update kernel");
+    check(cg_pupdate_launch(vg, m_stream, n4, m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
+          "p kernel");
+    check(cudaStreamEndCapture(m_stream, &body), "capture body end");
+    check(cudaGraphInstantiate(&m_exec, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    m_execGen = m_generation;
+}
+
+Results PcgHandle::run(uint32_t maxIter, double tol) {
+    if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
+    // Records: slot 0 + one per iteration, up to a ring of kMaxRecords.
+    const uint64_t want = std::min<uint64_t>((uint64_t)maxIter + 2, kMaxRecords);
+    if (want > m_recCap) {
+        alloc(m_records, sizeof(IterRecord) * want, "iteration records");
+        m_recCap = want;
+    }
+    check(cudaMemsetAsync(m_records.p, 0, sizeof(IterRecord) * std::min<uint64_t>(m_recCap, want), m_stream),
+          "memset records");
+    CgState cmd = {};
+    cmd.tol = tol;
+    cmd.maxIterP1 = maxIter + 1u;
+    cmd.records = m_records.as<IterRecord>();
+    cmd.recCap = (uint32_t)want;
+    const int n = (int)m_n, n4 = (int)m_n4;
+    CgState* st = m_state.as<CgState>();
+    double* part = m_partials.as<double>();
+    if (m_useGraph) {
+        buildGraph();
+        cmd.useCond = 1;
+        cmd.condHandle = (uint64_t)m_cond;
+    }
+    check(cudaMemcpyAsync(st, &cmd, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
+    check(cudaEventRecord(m_ev0, m_stream), "event");
+    if (m_useGraph) {
+        check(cudaGraphLaunch(m_exec, m_stream), "graph launch");
+    } else {
+        // Host-driven loop: batches of iterations, kernels skip once done.
+        const int vg = vec_grid(n4, m_numSms);
+        check(cg_init_launch(vg, m_stream, n, n4, m_b.as<double>(), m_diag.as<double>(), m_x.as<double>(),
+                             m_r.as<double>(), m_p.as<double>(), m_J.as<double>(), m_Ap.as<double>(), st, part),
+              "init kernel");
+        uint64_t ran = 0;
+        for (;;) {
+            for (int u = 0; u < 16; ++u) {
+                check(spmv_launch<double>(m_spmvCfg, m_spmvGrid, m_stream, n, m_rowptr.as<int>(), m_col.as<int>(),
+                                          m_val.as<double>(), m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part,
+                                          kSpmvCgDot, &st->done),
+                      "SpMV kernel");
+                check(cg_update_launch(vg, m_stream, n4, m_x.as<double>(), m_r.as<double>(), m_p.as<double>(),
+                                       m_Ap.as<double>(), m_J.as<double>(), st, part),
+                      "update kernel");
+                check(cg_pupdate_launch(vg, m_stream, n4, m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
+                      "p kernel");
+            }
+            ran += 16;
+            uint32_t done = 0;
+            check(cudaMemcpyAsync(&done, &st->done, sizeof(uint32_t), cudaMemcpyDeviceToHost, m_stream), "D2H");
+            check(cudaStreamSynchronize(m_stream), "sync");
+            if (done || ran > (uint64_t)maxIter + 1) break;
+        }
+    }
+    check(cudaEventRecord(m_ev1, m_stream), "event");
+    check(cudaMemcpyAsync(&m_lastState, st, sizeof(CgState), cudaMemcpyDeviceToHost, m_stream), "state download");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    check(cudaEventElapsedTime(&m_lastMs, m_ev0, m_ev1), "event");
+    return readResults(maxIter);
+}
+
+Results PcgHandle::readResults(uint32_t maxIter) {
+    const CgState& s = m_lastState;
+    if (s.status & kStatusWaitTimeout) throw InternalError("Run kernel failed: a device wait timed out.");
+    Results r;
+    r.itersRun = s.k;
+    // pcgImp.hpp:171-180: the scan stops at the first empty record, so a run
+    // that used all maxIter + 1 slots reports maxIter.
+    r.reportedIters = s.k <= maxIter ? s.k : maxIter;
+    r.rrLast = s.rr;
+    r.bb = s.bb;
+    r.status = s.status;
+    m_lastBb = s.bb;
+    return r;
+}
+
+void PcgHandle::copyX(double* x, uint32_t n, bool toDevice) {
+    check(cudaMemcpyAsync(x, m_x.p, sizeof(double) * n, toDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          m_stream),
+          "copy x");
+    check(cudaStreamSynchronize(m_stream), "sync");
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision
+// ---------------------------------------------------------------------------
+void PcgHandle::buildMixedGraph() {
+    if (m_mixedExec && m_mixedGen == m_generation) return;
+    if (m_mixedExec) {
+        cudaGraphExecDestroy(m_mixedExec);
+        m_mixedExec = nullptr;
+    }
+    const int n = (int)m_n, n4 = (int)m_n4;
+    const int vg = vec_grid(n4, m_numSms);
+    const int cfg32 = m_spmvCfg;
+    const int grid32 = spmv_grid<float>(cfg32, n, m_numSms);
+    CgState* st = m_state.as<CgState>();
+    CgState* in = m_state32.as<CgState>();
+    double* part = m_partials.as<double>();
+    const double innerTol = envDouble("XJPCG_INNER_TOL", 1e-5);
+    cudaGraph_t g = nullptr;
+    check(cudaGraphCreate(&g, 0), "cudaGraphCreate");
+    check(cudaStreamBeginCaptureToGraph(m_stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+          "capture");
+    check(ir_init_launch(vg, m_stream, n, n4, m_b.as<double>(), m_diag.as<double>(), m_x.as<double>(),
+                         m_J32.as<float>(), st, part),
+          "ir init");
+    check(cudaStreamEndCapture(m_stream, &g), "capture end");
+    size_t nn = 0;
+    check(cudaGraphGetNodes(g, nullptr, &nn), "nodes");
+    std::vector<cudaGraphNode_t> nodes(nn);
+    check(cudaGraphGetNodes(g, nodes.data(), &nn), "nodes");
+    check(cudaGraphConditionalHandleCreate(&m_condOuter, g, 1, cudaGraphCondAssignDefault), "handle");
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = m_condOuter;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t outerNode;
+    check(cudaGraphAddNode(&outerNode, g, nodes.data(), nullptr, nn, &cp), "outer node");
+    cudaGraph_t outerBody = cp.conditional.phGraph_out[0];
+
+    // outer body part 1: residual, check, inner init
+    check(cudaGraphConditionalHandleCreate(&m_condInner, outerBody, 0, 0), "handle");
+    check(cudaStreamBeginCaptureToGraph(m_stream, outerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+          "capture");
+    check(spmv_launch<double>(m_spmvCfg, m_spmvGrid, m_stream, n, m_rowptr.as<int>(), m_col.as<int>(),
+                              m_val.as<double>(), m_x.as<double>(), m_r.as<double>(), m_b.as<double>(), st, part,
+                              kSpmvResidual, nullptr),
+          "residual SpMV");
+    check(ir_check_launch(m_stream, st, in, (uint64_t)m_condOuter, kMaxOuter), "ir check");
+    check(ir_inner_init_launch(vg, m_stream, n4, m_r.as<double>(), m_J32.as<float>(), m_r32.as<float>(),
+                               m_p32.as<float>(), m_d32.as<float>(), st, in, part, (uint64_t)m_condInner, innerTol),
+          "inner init");
+    check(cudaStreamEndCapture(m_stream, &outerBody), "capture end");
+    size_t on = 0;
+    check(cudaGraphGetNodes(outerBody, nullptr, &on), "nodes");
+    std::vector<cudaGraphNode_t> onodes(on);
+    check(cudaGraphGetNodes(outerBody, onodes.data(), &on), "nodes");
+    // The leaf of the outer body so far is the inner-init node: find nodes
+    // without dependents.
+    std::vector<cudaGraphNode_t> leaves;
+    for (auto nd : onodes) {
+        size_t cnt = 0;
+        check(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &cnt), "deps");
+        if (cnt == 0) leaves.push_back(nd);
+    }
+    cudaGraphNodeParams ip = {};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = m_condInner;
+    ip.conditional.type = cudaGraphCondTypeWhile;
+    ip.conditional.size = 1;
+    cudaGraphNode_t innerNode;
+    check(cudaGraphAddNode(&innerNode, outerBody, leaves.data(), nullptr, leaves.size(), &ip), "inner node");
+    cudaGraph_t innerBody = ip.conditional.phGraph_out[0];
+    check(cudaStreamBeginCaptureToGraph(m_stream, innerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+          "capture");
+    check(spmv_launch<float>(cfg32, grid32, m_stream, n, m_rowptr.as<int>(), m_col.as<int>(), m_val32.as<float>(),
+                             m_p32.as<float>(), m_Ap32.as<float>(), nullptr, in, part, kSpmvCgDot, &in->done),
+          "SpMV fp32");
+    check(cg32_update_launch(vg, m_stream, n4, m_d32.as<float>(), m_r32.as<float>(), m_p32.as<float>(),
+                             m_Ap32.as<float>(), m_J32.as<float>(), in, part, (uint64_t)m_condInner, 1),
+          "update fp32");
+    check(cg32_pupdate_launch(vg, m_stream, n4, m_p32.as<float>(), m_r32.as<float>(), m_J32.as<float>(), in),
+          "p fp32");
+    check(cudaStreamEndCapture(m_stream, &innerBody), "capture end");
+    // outer body part 2: x update after the inner loop
+    check(cudaStreamBeginCaptureToGraph(m_stream, outerBody, &innerNode, nullptr, 1, cudaStreamCaptureModeThreadLocal),
+          "capture");
+    check(ir_update_launch(vg, m_stream, n4, m_x.as<double>(), m_d32.as<float>(), st, in), "ir update");
+    check(cudaStreamEndCapture(m_stream, &outerBody), "capture end");
+    check(cudaGraphInstantiate(&m_mixedExec, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    m_mixedGen = m_generation;
+}
+
+Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
+    if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
+    const size_t vb32 = sizeof(float) * ((size_t)m_n4 + 4);
+    alloc(m_r32, vb32, "r32");
+    alloc(m_p32, vb32, "p32");
+    alloc(m_d32, vb32, "d32");
+    alloc(m_Ap32, vb32, "Ap32");
+    alloc(m_J32, vb32, "J32");
+    const uint64_t nnzPad = (m_nnz + 3) / 4 * 4 + 4;
+    if (!m_val32Valid) {
+        alloc(m_val32, sizeof(float) * nnzPad, "fp32 values");
+        check(convert_f64_to_f32(m_stream, (int64_t)nnzPad, m_val.as<double>(), m_val32.as<float>()), "fp32 values");
+        m_val32Valid = true;
+    }
+    check(cudaMemsetAsync(m_p32.p, 0, vb32, m_stream), "memset");
+    check(cudaMemsetAsync(m_Ap32.p, 0, vb32, m_stream), "memset");
+    CgState* st = m_state.as<CgState>();
+    CgState* in = m_state32.as<CgState>();
+    CgState cmd = {};
+    cmd.tol = tol;
+    cmd.maxIterP1 = maxIter + 1u;
+    cmd.useCond = 1;
+    CgState cmdIn = {};
+    cmdIn.useCond = 1;
+    buildMixedGraph();
+    check(cudaMemcpyAsync(st, &cmd, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
+    check(cudaMemcpyAsync(in, &cmdIn, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
+    check(cudaEventRecord(m_ev0, m_stream), "event");
+    check(cudaGraphLaunch(m_mixedExec, m_stream), "graph launch");
+    check(cudaEventRecord(m_ev1, m_stream), "event");
+    check(cudaMemcpyAsync(&m_lastState, st, sizeof(CgState), cudaMemcpyDeviceToHost, m_stream), "state download");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    check(cudaEventElapsedTime(&m_lastMs, m_ev0, m_ev1), "event");
+    const CgState& s = m_lastState;
+    if (s.status & kStatusWaitTimeout) throw InternalError("Run kernel failed: a device wait timed out.");
+    m_lastOuter = s.outer;
+    m_lastInner = s.innerK;
+    Results r;
+    r.itersRun = s.innerK;
+    r.reportedIters = s.innerK;
+    r.rrLast = s.rr;
+    r.bb = s.bb;
+    r.status = s.status;
+    m_lastBb = s.bb;
+    return r;
+}
+
+void PcgHandle::copyX64(double* x, uint32_t n, bool toDevice) { copyX(x, n, toDevice); }
+
+// ---------------------------------------------------------------------------
+// Utilities
+// ---------------------------------------------------------------------------
+void PcgHandle::spmv(const double* x, double* y, bool onDevice) {
+    if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
+    const double* dx = x;
+    double* dy = y;
+    if (!onDevice) {
+        alloc(m_scratchY, sizeof(double) * ((size_t)m_n4 + 4), "SpMV output");
+        check(cudaMemcpyAsync(m_b.p, x, sizeof(double) * m_n, cudaMemcpyHostToDevice, m_stream), "H2D x");
+        dx = m_b.as<double>();
+        dy = m_scratchY.as<double>();
+    }
+    check(spmv_launch<double>(m_spmvCfg, m_spmvGrid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
+                              m_val.as<double>(), dx, dy, nullptr, m_state.as<CgState>(), m_partials.as<double>(),
+                              kSpmvPlain, nullptr),
+          "SpMV");
+    if (!onDevice) {
+        check(cudaMemcpyAsync(y, dy, sizeof(double) * m_n, cudaMemcpyDeviceToHost, m_stream), "D2H y");
+        check(cudaStreamSynchronize(m_stream), "sync");
+    }
+}
+
+void PcgHandle::getCsr(int32_t* rowPtr, int32_t* colIdx, double* values, uint32_t* perm) {
+    if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
+    if (rowPtr)
+        check(cudaMemcpyAsync(rowPtr, m_rowptr.p, sizeof(int) * ((size_t)m_n + 1), cudaMemcpyDeviceToHost, m_stream),
+              "D2H");
+    if (colIdx) check(cudaMemcpyAsync(colIdx, m_col.p, sizeof(int) * m_nnz, cudaMemcpyDeviceToHost, m_stream), "D2H");
+    if (values)
+        check(cudaMemcpyAsync(values, m_val.p, sizeof(double) * m_nnz, cudaMemcpyDeviceToHost, m_stream), "D2H");
+    if (perm) check(cudaMemcpyAsync(perm, m_perm.p, sizeof(uint32_t) * m_nnz, cudaMemcpyDeviceToHost, m_stream), "D2H");
+    check(cudaStreamSynchronize(m_stream), "sync");
+}
+
+uint64_t PcgHandle::getRecords(void* buf, uint64_t cap) {
+    if (m_recCap == 0) return 0;
+    const uint64_t used = std::min<uint64_t>((uint64_t)m_lastState.k + 1, m_recCap);
+    const uint64_t cnt = std::min<uint64_t>(used, cap);
+    check(cudaMemcpyAsync(buf, m_records.p, sizeof(IterRecord) * cnt, cudaMemcpyDeviceToHost, m_stream), "D2H");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    return cnt;
+}
+
+void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
+    std::memset(info, 0, sizeof(*info));
+    info->n = m_n;
+    info->n4 = m_n4;
+    info->nnz = m_nnz;
+    info->itersRun = m_lastState.k;
+    info->spmvLanes = (uint32_t)spmv_config_lanes(m_spmvCfg);
+    info->spmvGrid = (uint32_t)m_spmvGrid;
+    info->statusBits = m_lastState.status;
+    info->outerSweeps = m_lastOuter;
+    info->innerIters = m_lastInner;
+    info->bb = m_lastState.bb;
+    info->rrLast = m_lastState.rr;
+    info->solveMs = m_lastMs;
+    info->loopMode = m_useGraph ? 1u : 0u;
+}
+
+}  // namespace xjpcg

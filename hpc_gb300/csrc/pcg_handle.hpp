@@ -1,0 +1,170 @@
+// pcg_handle.hpp -- the object behind an XJPCG_Handle_t.
+//
+// Mirrors the reference's PCGImpl (pcg/sw/include/impl/pcgImp.hpp:44-253):
+// matrix set / values-only update / reuse, vector set, run, result, metrics,
+// last status and message.  The FPGA runtime underneath it (xCgHost,
+// pcg/sw/src/cgHost.cpp:356-496) becomes a CUDA stream, device buffers and a
+// CUDA graph that holds the whole solve: the vector-init kernel followed by a
+// conditional WHILE node whose body is the three per-iteration kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pcg.h"
+#include "../../include/xjpcg_gb300.h"
+#include "xjpcg_state.h"
+#include "xjpcg_internal.hpp"
+
+namespace xjpcg {
+
+// Exceptions carry the status they map to; messages use the reference's
+// prefixes (pcg/sw/include/impl/cgException.hpp:36-54).
+class CgError : public std::runtime_error {
+   public:
+    CgError(XJPCG_Status_t st, const std::string& msg) : std::runtime_error(msg), status(st) {}
+    XJPCG_Status_t status;
+};
+inline CgError InvalidValue(const std::string& s) { return CgError(XJPCG_STATUS_INVALID_VALUE, "INVALID VALUE ERROR: " + s); }
+inline CgError InternalError(const std::string& s) { return CgError(XJPCG_STATUS_INTERNAL_ERROR, "INTERNAL ERROR: " + s); }
+inline CgError AllocFailed(const std::string& s) { return CgError(XJPCG_STATUS_ALLOC_FAILED, "Alloc Failed ERROR: " + s); }
+inline CgError ExecFailed(const std::string& s) { return CgError(XJPCG_STATUS_EXECUTION_FAILED, "Solver ERROR: " + s); }
+
+// Grow-only device buffer.  Every reallocation bumps the owner's generation
+// so graphs that captured the old address are rebuilt.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    bool ensure(size_t b, uint64_t* generation);
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+struct Results {
+    uint32_t reportedIters;  // min(K, maxIter), the reference's host scan
+    uint32_t itersRun;       // K
+    double rrLast;
+    double bb;
+    uint32_t status;
+};
+
+class PcgHandle {
+   public:
+    PcgHandle() = default;
+    ~PcgHandle();
+    void init();
+
+    // Matrix input.  base: 0 = C, 1 = Fortran (mode >> 4).
+    void setCooMat(uint32_t n, uint64_t nnz, const uint32_t* row, const uint32_t* col, const double* data, int base);
+    void updateCooValues(uint32_t n, uint64_t nnz, const double* data);
+    void setCscSymMat(uint32_t n, uint64_t nnzHalf, const int64_t* rowIdx, const int64_t* colPtr, const double* data,
+                      int base);
+    void updateCscSymValues(uint32_t n, uint64_t nnzHalf, const int64_t* rowIdx, const int64_t* colPtr,
+                            const double* data, int base);
+    void setCsrMat(uint32_t n, uint64_t nnz, const int32_t* rowPtr, const int32_t* colIdx, const double* data,
+                   int base);
+    void updateCsrValues(uint32_t n, uint64_t nnz, const double* data);
+
+    void setVec(uint32_t n, const double* b, const double* diag, bool onDevice);
+    Results run(uint32_t maxIter, double tol);
+    void copyX(double* x, uint32_t n, bool toDevice);
+
+    Results runMixed(uint32_t maxIter, double tol);
+    void copyX64(double* x, uint32_t n, bool toDevice);
+
+    void spmv(const double* x, double* y, bool onDevice);
+    void getCsr(int32_t* rowPtr, int32_t* colIdx, double* values, uint32_t* perm);
+    uint64_t getRecords(void* buf, uint64_t cap);
+    void fillInfo(XJPCG_GbInfo_t* info) const;
+    void setLanes(int lanes);
+
+    bool hasMatrix() const { return m_haveMatrix; }
+    uint32_t matrixN() const { return m_n; }
+    cudaStream_t stream() const { return m_stream; }
+
+    XJPCG_Metric_t* metrics() { return &m_metrics; }
+    const XJPCG_Metric_t* metrics() const { return &m_metrics; }
+    XJPCG_Status_t setStatusMessage(XJPCG_Status_t st, const std::string& msg) const {
+        m_lastStatus = st;
+        m_lastMessage = msg;
+        return st;
+    }
+    XJPCG_Status_t lastStatus() const { return m_lastStatus; }
+    const std::string& lastMessage() const { return m_lastMessage; }
+    bool isFirstCall() const { return m_firstCall; }
+    void markCalled() { m_firstCall = false; }
+    double dot() const { return m_lastBb; }
+
+   private:
+    void check(cudaError_t e, const char* what);
+    void alloc(DevBuf& b, size_t bytes, const char* what);
+    void finishMatrix();     // after CSR exists: values pad, tuning
+    void tuneSpmv();
+    void ensureVectors(uint32_t n);
+    void buildGraph();
+    void buildMixedGraph();
+    Results readResults(uint32_t maxIter);
+
+    mutable XJPCG_Status_t m_lastStatus = XJPCG_STATUS_SUCCESS;
+    mutable std::string m_lastMessage;
+    bool m_firstCall = true;
+    XJPCG_Metric_t m_metrics = {0, 0, 0, 0};
+
+    int m_device = 0;
+    int m_numSms = 0;
+    cudaStream_t m_stream = nullptr;
+    cudaEvent_t m_ev0 = nullptr, m_ev1 = nullptr;
+    uint64_t m_generation = 1;
+
+    // matrix
+    bool m_haveMatrix = false;
+    uint32_t m_n = 0;
+    uint64_t m_nnz = 0;
+    uint64_t m_nnzHalf = 0;   // symmetric CSC input only
+    int m_kind = 0;           // 0 none, 1 COO, 2 CSC-sym, 3 CSR
+    DevBuf m_rowptr, m_col, m_val, m_perm, m_val32;
+    DevBuf m_inRow, m_inCol, m_inVal, m_inIdx64, m_inPtr64;
+    DevBuf m_counts, m_fill, m_blockSums, m_keys, m_flags, m_cscScratch;
+    bool m_val32Valid = false;
+    int m_forcedLanes = 0;
+    int m_spmvCfg = 2;
+    int m_spmvGrid32Cfg = 2;
+    int m_spmvGrid = 0;
+
+    // vectors
+    uint32_t m_vecN = 0, m_n4 = 0;
+    DevBuf m_b, m_diag, m_x, m_r, m_p, m_J, m_Ap;
+    DevBuf m_state, m_partials, m_records;
+    uint64_t m_recCap = 0;
+    DevBuf m_scratchY;
+    // mixed precision
+    DevBuf m_state32, m_r32, m_p32, m_d32, m_Ap32, m_J32;
+
+    // graph
+    cudaGraphExec_t m_exec = nullptr;
+    uint64_t m_execGen = 0;
+    cudaGraphConditionalHandle m_cond = 0;
+    cudaGraphExec_t m_mixedExec = nullptr;
+    uint64_t m_mixedGen = 0;
+    cudaGraphConditionalHandle m_condOuter = 0, m_condInner = 0;
+    bool m_useGraph = true;
+
+    // last results
+    double m_lastBb = 0.0;
+    CgState m_lastState{};
+    float m_lastMs = 0.f;
+    uint32_t m_lastOuter = 0, m_lastInner = 0;
+};
+
+}  // namespace xjpcg

@@ -1,0 +1,147 @@
+// xjpcg_device.cuh -- device-side building blocks shared by the xJPCG kernels:
+// the per-handle solver state, deterministic block/grid reductions, and the
+// mbarrier + cp.async.bulk primitives (inline PTX, sm_103a) with bounded waits.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "xjpcg_state.h"
+
+namespace xjpcg {
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic reductions.  Every sum below has a fixed association order for
+// a fixed launch shape, so results are bitwise stable run to run.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of NV values per thread; result valid in thread 0.
+template <int NT, int NV, typename T>
+__device__ __forceinline__ void block_sum(T (&v)[NV]) {
+    __shared__ T red[NV][NT / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) red[i][wid] = v[i];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            T s = lane < NT / 32 ? red[i][lane] : T(0);
+            v[i] = warp_sum(s);
+        }
+    }
+    __syncthreads();
+}
+
+// Last-block-done grid reduction of NV doubles.  Each block calls it once with
+// its block total in thread 0.  Returns true in the block that finished last;
+// in that block, out[] holds the grid totals (valid in all threads).  The
+// partial buffer must hold NV * gridDim.x doubles.
+template <int NV>
+__device__ __forceinline__ bool grid_sum_last(const double (&blockTotal)[NV], double* partials,
+                                              uint32_t* counter, double (&out)[NV]) {
+    __shared__ bool amLast;
+    __shared__ double fin[NV];
+    const int nb = gridDim.x;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) partials[i * nb + blockIdx.x] = blockTotal[i];
+        __threadfence();
+        uint32_t ticket = atomicAdd(counter, 1u);
+        amLast = (ticket == (uint32_t)nb - 1);
+    }
+    __syncthreads();
+    if (!amLast) return false;
+    __threadfence();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = 0.0;
+            for (int b = lane; b < nb; b += 32) s += __ldcg(&partials[i * nb + b]);
+            s = warp_sum(s);
+            if (lane == 0) fin[i] = s;
+        }
+        if (lane == 0) *counter = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) out[i] = fin[i];
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier and bulk-copy primitives (PTX ISA 8.x, sm_90 and later).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the given phase parity.  Gives up after budgetNs of wall time and
+// returns false; the caller records kStatusWaitTimeout and winds down.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t budgetNs) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t spin = 0;; ++spin) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((spin & 255u) == 255u && globaltimer_ns() - t0 > budgetNs) return false;
+    }
+}
+
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// 1-D bulk copy global -> shared, completing on the mbarrier's transaction
+// count.  dst, src and bytes must all be multiples of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+        : "memory");
+}
+
+}  // namespace xjpcg

@@ -1,0 +1,65 @@
+// xjpcg_internal.hpp -- host-visible declarations of the device launchers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace xjpcg {
+
+struct CgState;
+
+// ---- SpMV (spmv_kernels.cu) ----
+int spmv_num_configs();
+int spmv_config_lanes(int cfg);
+template <typename VT>
+int spmv_grid(int cfg, int n, int numSms);
+template <typename VT>
+cudaError_t spmv_launch(int cfg, int grid, cudaStream_t st, int n, const int* rowptr, const int* col, const VT* val,
+                        const VT* x, VT* y, const VT* b, CgState* state, double* partials, int mode,
+                        const uint32_t* doneFlag);
+enum : int { kSpmvPlain = 0, kSpmvCgDot = 1, kSpmvResidual = 2 };
+
+// ---- CG vector kernels (cg_kernels.cu) ----
+int vec_grid(int n4, int numSms);
+cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x,
+                           double* r, double* p, double* J, double* Ap, CgState* state, double* partials);
+cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* x, double* r, const double* p,
+                             const double* Ap, const double* J, CgState* state, double* partials);
+cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* p, const double* r, const double* J,
+                              CgState* state);
+
+// ---- mixed precision (mixed_kernels.cu) ----
+cudaError_t ir_init_launch(int grid, cudaStream_t s, int n, int n4, const double* b, const double* diag, double* x,
+                           float* J32, CgState* st, double* partials);
+cudaError_t ir_check_launch(cudaStream_t s, CgState* st, CgState* in, uint64_t outerHandle, uint32_t maxOuter);
+cudaError_t ir_inner_init_launch(int grid, cudaStream_t s, int n4, const double* r64, const float* J32, float* r32,
+                                 float* p32, float* d32, CgState* st, CgState* in, double* partials,
+                                 uint64_t innerHandle, double innerTol);
+cudaError_t cg32_update_launch(int grid, cudaStream_t s, int n4, float* d, float* r, const float* p, const float* Ap,
+                               const float* J, CgState* in, double* partials, uint64_t innerHandle, int useCond);
+cudaError_t cg32_pupdate_launch(int grid, cudaStream_t s, int n4, float* p, const float* r, const float* J,
+                                CgState* in);
+cudaError_t ir_update_launch(int grid, cudaStream_t s, int n4, double* x, const float* d, CgState* st,
+                             const CgState* in);
+
+// ---- conversion (convert_kernels.cu) ----
+// All return cudaSuccess or the first CUDA error; data errors are reported
+// through *errFlag (device int) as kStatusIndexError / kStatusCountError.
+struct ConvertScratch {
+    int* counts = nullptr;      // n + 1
+    int* fill = nullptr;        // n
+    int* blockSums = nullptr;   // scan scratch
+    uint64_t* keys = nullptr;   // nnz
+    int* flags = nullptr;       // device int flags[4]
+    size_t countsCap = 0, keysCap = 0, blockCap = 0;
+};
+cudaError_t scan_exclusive(cudaStream_t st, const int* in, int* out, int count, int* blockSums);
+int scan_block_count(int count);
+cudaError_t coo_to_csr(cudaStream_t st, int n, int64_t nnz, const uint32_t* row, const uint32_t* col, int base,
+                       int* rowptr, int* colOut, uint32_t* perm, ConvertScratch& scratch, int* hostErr);
+cudaError_t gather_values(cudaStream_t st, int64_t nnz, const uint32_t* perm, const double* src, double* dst);
+cudaError_t cscsym_expand(cudaStream_t st, int n, int64_t nnzHalf, int64_t nnzFull, const int64_t* rowIdx,
+                          const int64_t* colPtr, const double* data, int base, uint32_t* rowOut, uint32_t* colOut,
+                          double* valOut, int64_t* posScratch, int* flagScratch, int* blockSums, int* hostErr);
+cudaError_t convert_f64_to_f32(cudaStream_t st, int64_t count, const double* src, float* dst);
+
+}  // namespace xjpcg

@@ -1,0 +1,48 @@
+// xjpcg_state.h -- plain structs shared by host and device code: the
+// per-solve device state and the 64-byte iteration record.
+#pragma once
+#include <cstdint>
+
+namespace xjpcg {
+
+// Status bits written by kernels into CgState::status.
+enum : uint32_t {
+    kStatusBreakdown = 1u,    // alpha, beta or r.r became non-finite
+    kStatusWaitTimeout = 2u,  // an mbarrier wait ran out of its time budget
+    kStatusIndexError = 4u,   // a matrix index was outside [0, n)
+    kStatusCountError = 8u,   // symmetric expansion produced the wrong count
+};
+
+// One 64-byte iteration record, laid out like the reference's CGSolverInstr
+// memory image (pcg/hw/include/impl/cgInstr.hpp:117-132):
+// u32 ID, Iter, VecSize, MaxIter; f64 Tols, Res, RZ, Alpha, Beta; u64 Clock.
+struct alignas(8) IterRecord {
+    uint32_t id, iter, vecSize, maxIter;
+    double tols, res, rz, alpha, beta;
+    uint64_t clock;
+};
+static_assert(sizeof(IterRecord) == 64, "record must be 64 bytes");
+
+// Per-solve state in device memory.  The host writes the command fields
+// (tol, maxIterP1, records, recCap) before each graph launch; the kernels
+// own the rest.  Reductions use counters[] for the last-block-done pattern.
+struct alignas(16) CgState {
+    double rz, pAp, alpha, beta, rr, bb, tols, tol;
+    double rrTrue;                 // mixed precision: true residual norm^2
+    double scale;                  // mixed precision: inner rhs scale
+    uint32_t k;                    // iterations run so far (K)
+    uint32_t maxIterP1;            // MaxIter of the record: user maxIter + 1
+    uint32_t done;                 // 1 once the loop must stop
+    uint32_t status;               // kStatus* bits
+    uint32_t vecSize;              // n rounded up to a multiple of 4
+    uint32_t recCap;               // slots in records[]
+    uint32_t counters[6];          // last-block-done tickets
+    IterRecord* records;           // slot 0 = command, slot k+1 = iteration k
+    uint64_t condHandle;           // cudaGraphConditionalHandle of the loop
+    uint32_t useCond;              // 1 when running under a conditional node
+    uint32_t outer;                // mixed precision: refinement sweeps
+    uint32_t innerK;               // mixed precision: inner iterations total
+    uint32_t pad;
+};
+
+}  // namespace xjpcg

@@ -1,0 +1,296 @@
+"""Parity of the CUDA JPCG path against the oracle, through the C ABI.
+
+Bar (from the workload contract): true ||b - A x|| / ||b|| <= 1e-10,
+||x - x_oracle|| / ||x_oracle|| <= 1e-8, iteration count within 1 % of the
+oracle's; integer/index outputs (CSR conversion, iteration counters, record
+fields) bit-exact.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import hpc_gb300 as X
+import oracle
+from hpc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+X_TOL = 1e-8      # ||x - x_ref|| / ||x_ref||
+RES_TOL = 1e-10   # true relative residual
+
+
+def _check_solve(sysm, r, tol=1e-10, max_iter=20000):
+    ref = oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, max_iter, tol)
+    assert r.status == X.SUCCESS, r.message
+    assert abs(r.iters - ref["iters"]) <= max(1, int(0.01 * ref["iters"])), (r.iters, ref["iters"])
+    err = np.linalg.norm(r.x - ref["x"]) / np.linalg.norm(ref["x"])
+    assert err <= X_TOL, err
+    rel = oracle.true_relres(sysm.rowptr, sysm.col, sysm.val, sysm.b, r.x)
+    assert rel <= RES_TOL * 1.5, rel
+    assert r.res <= tol
+    return ref
+
+
+def test_poisson7_32_coo(handle):
+    s = W.poisson7(32)
+    rows, cols, vals = s.coo()
+    r = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 2000, 1e-10)
+    _check_solve(s, r, max_iter=2000)
+
+
+def test_diffusion27_small_csr(handle):
+    s = W.diffusion27(20, sigma=1.5, seed=1)
+    r = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
+    _check_solve(s, r)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
+def test_every_spmv_shape_solves(handle, lanes):
+    s = W.diffusion27(12, sigma=1.5, seed=7)
+    rows, cols, vals = s.coo()
+    handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 5, 1e-10)  # set the matrix
+    handle.set_spmv_lanes(lanes)
+    r = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 20000, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    assert handle.info().spmvLanes == lanes
+    _check_solve(s, r)
+
+
+def test_conversion_bitexact_unsorted_fortran(handle):
+    rng = np.random.default_rng(11)
+    s = W.diffusion27(10, seed=3)
+    rows, cols, vals = s.coo()
+    # shuffle, add exact duplicates split in two, switch to 1-based
+    perm = rng.permutation(rows.size)
+    rows, cols, vals = rows[perm], cols[perm], vals[perm]
+    dup = rng.choice(rows.size, 50, replace=False)
+    half = vals[dup] / 2
+    vals = vals.copy()
+    vals[dup] = half
+    rows = np.concatenate([rows, rows[dup]])
+    cols = np.concatenate([cols, cols[dup]])
+    vals = np.concatenate([vals, half])
+    r = handle.coo_solve(s.n, rows + 1, cols + 1, vals, s.diag, s.b, 20000, 1e-10,
+                         mode=X.MODE_DEFAULT | X.MODE_FORTRAN_INDEX)
+    assert r.status == X.SUCCESS, r.message
+    rp, ci, v, pm = handle.get_csr()
+    orp, oci, opm = oracle.coo_to_csr(s.n, rows + 1, cols + 1, base=1)
+    assert np.array_equal(rp, orp)
+    assert np.array_equal(ci, oci)
+    assert np.array_equal(pm, opm)
+    assert np.array_equal(v, vals[opm])
+
+
+def test_conversion_long_rows(handle):
+    # rows longer than 32 and 4096 exercise the CTA sorters and multi-chunk SpMV
+    rng = np.random.default_rng(12)
+    n = 9000
+    rows = [np.arange(n)]
+    cols = [np.arange(n)]
+    for r_, L in [(5, 6000), (77, 300), (4000, 40), (8999, 5000)]:
+        c = rng.choice(n, L, replace=False)
+        rows.append(np.full(L, r_))
+        cols.append(c)
+    rows = np.concatenate(rows).astype(np.uint32)
+    cols = np.concatenate(cols).astype(np.uint32)
+    perm = rng.permutation(rows.size)
+    rows, cols = rows[perm], cols[perm]
+    vals = rng.standard_normal(rows.size)
+    diag = np.ones(n)
+    b = rng.uniform(-1, 1, n)
+    # A non-SPD matrix: only the conversion and the SpMV are checked.
+    handle.coo_solve(n, rows, cols, vals, diag, b, 1, 1e-10)
+    rp, ci, v, pm = handle.get_csr()
+    orp, oci, opm = oracle.coo_to_csr(n, rows, cols)
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci) and np.array_equal(pm, opm)
+    x = rng.standard_normal(n)
+    for lanes in [1, 4, 32]:
+        handle.set_spmv_lanes(lanes)
+        y = handle.spmv(x)
+        yref = oracle.spmv(orp, oci, vals[opm], x)
+        scale = oracle.spmv(orp, oci, np.abs(vals[opm]), np.abs(x))
+        assert np.all(np.abs(y - yref) <= 1e-13 * scale + 1e-300)
+
+
+def test_cscsym_bitexact(handle):
+    s = W.poisson7(12)
+    A_rows, A_cols, A_vals = s.coo()
+    lower = A_rows >= A_cols
+    # lower triangle as CSC: column-major order of (row >= col) entries
+    r, c, v = A_rows[lower], A_cols[lower], A_vals[lower]
+    order = np.lexsort((r, c))
+    r, c, v = r[order], c[order], v[order]
+    colptr = np.zeros(s.n + 1, np.int64)
+    np.cumsum(np.bincount(c, minlength=s.n), out=colptr[1:])
+    for base in (0, 1):
+        mode = X.MODE_DEFAULT | (X.MODE_FORTRAN_INDEX if base else 0)
+        res = handle.csc_sym_solve(s.n, r.astype(np.int64) + base, colptr + base, v, s.diag, s.b, 2000, 1e-10,
+                                   mode=mode)
+        assert res.status == X.SUCCESS, res.message
+        er, ec, ev = oracle.cscsym_expand(s.n, r.astype(np.int64) + base, colptr + base, v, base=base)
+        orp, oci, opm = oracle.coo_to_csr(s.n, er, ec)
+        rp, ci, vv, pm = handle.get_csr()
+        assert np.array_equal(rp, orp) and np.array_equal(ci, oci) and np.array_equal(pm, opm)
+        assert np.array_equal(vv, ev[opm])
+        _check_solve(s, res, max_iter=2000)
+
+
+def test_spmv_matches_oracle(handle):
+    s = W.diffusion27(24, seed=5)
+    rows, cols, vals = s.coo()
+    handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 1, 1e-10)
+    x = np.random.default_rng(1).standard_normal(s.n)
+    y = handle.spmv(x)
+    yref = oracle.spmv(s.rowptr, s.col, s.val, x)
+    scale = oracle.spmv(s.rowptr, s.col, np.abs(s.val), np.abs(x))
+    assert np.all(np.abs(y - yref) <= 1e-13 * scale)
+
+
+def test_modes_and_reuse(handle):
+    s = W.poisson7(16)
+    rows, cols, vals = s.coo()
+    # reuse modes on the first call are INVALID_VALUE (pcg.cpp:84-95, 141-152)
+    r = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 100, 1e-10, mode=X.MODE_KEEP_NZ_LAYOUT)
+    assert r.status == X.INVALID_VALUE
+    r = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 100, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    assert r.status == X.INVALID_VALUE
+    r1 = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 2000, 1e-10)
+    assert r1.status == X.SUCCESS
+    # KEEP_NZ_LAYOUT with NULL indices and scaled values (example.c:81-82)
+    r2 = handle.coo_solve(s.n, None, None, vals * 2.0, s.diag * 2.0, s.b, 2000, 1e-10, mode=X.MODE_KEEP_NZ_LAYOUT)
+    assert r2.status == X.SUCCESS, r2.message
+    s2 = W.System(s.n, s.rowptr, s.col, s.val * 2.0, s.diag * 2.0, s.b)
+    _check_solve(s2, r2, max_iter=2000)
+    # KEEP_MATRIX with a new right-hand side
+    b3 = np.random.default_rng(3).uniform(-1, 1, s.n)
+    r3 = handle.coo_solve(s.n, None, None, None, s.diag * 2.0, b3, 2000, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    assert r3.status == X.SUCCESS, r3.message
+    s3 = W.System(s.n, s.rowptr, s.col, s.val * 2.0, s.diag * 2.0, b3)
+    _check_solve(s3, r3, max_iter=2000)
+    # wrong nnz on a values-only update -> INTERNAL_ERROR (checkUpdateDim)
+    r4 = handle.coo_solve(s.n, None, None, vals[:-1], s.diag, s.b, 10, 1e-10, nnz=vals.size - 1,
+                          mode=X.MODE_KEEP_NZ_LAYOUT)
+    assert r4.status == X.INTERNAL_ERROR
+
+
+def test_argument_errors(handle):
+    s = W.poisson7(8)
+    rows, cols, vals = s.coo()
+    assert handle.coo_solve(0, rows, cols, vals, s.diag, s.b, 10, 1e-10).status == X.INVALID_VALUE
+    assert handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 10, 1e-10, nnz=0).status == X.INVALID_VALUE
+    assert handle.coo_solve(s.n, rows, cols, None, s.diag, s.b, 10, 1e-10).status == X.INVALID_VALUE
+    assert handle.coo_solve(s.n, None, cols, vals, s.diag, s.b, 10, 1e-10).status == X.INVALID_VALUE
+    bad = rows.copy()
+    bad[3] = s.n
+    r = handle.coo_solve(s.n, bad, cols, vals, s.diag, s.b, 10, 1e-10)
+    assert r.status == X.INVALID_VALUE
+    r = handle.coo_solve(s.n, rows, cols, vals, None, s.b, 10, 1e-10)
+    assert r.status == X.INVALID_VALUE and "Vector is nullptr" in r.message
+    assert handle.last_status() == X.INVALID_VALUE
+    r = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 10, 1e-10, mode=0x20)
+    assert r.status == X.INTERNAL_ERROR
+
+
+def test_maxiter_cap_and_records(handle):
+    s = W.diffusion27(12, seed=9)
+    rows, cols, vals = s.coo()
+    for max_iter in (0, 1, 7):
+        r = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, max_iter, 1e-10)
+        ref = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, max_iter, 1e-10, records=True)
+        assert r.status == X.EXECUTION_FAILED
+        assert r.iters == ref["iters"] == max_iter
+        assert handle.info().itersRun == ref["k"] == max_iter + 1
+        assert abs(r.res - ref["res"]) <= 1e-9 * ref["res"]
+        recs = handle.records()
+        assert len(recs) == ref["k"] + 1
+        orec = ref["records"][:len(recs)]
+        for f in ("id", "iter", "vecSize", "maxIter"):
+            assert np.array_equal(recs[f], orec[f]), f
+        for f in ("tols", "res", "rz", "alpha", "beta"):
+            assert np.allclose(recs[f], orec[f], rtol=1e-9, atol=0), f
+
+
+def test_records_converged(handle):
+    s = W.poisson7(16)
+    rows, cols, vals = s.coo()
+    r = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 2000, 1e-10)
+    ref = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 2000, 1e-10, records=True)
+    recs = handle.records()
+    assert r.status == X.SUCCESS
+    assert len(recs) == r.iters + 1
+    assert recs["maxIter"][0] == 2001 and np.all(recs["maxIter"][1:] == 2001)
+    assert np.array_equal(recs["iter"][1:], np.arange(r.iters))
+    k = min(len(recs), ref["k"] + 1)
+    assert np.allclose(recs["res"][:k][:20], ref["records"]["res"][:k][:20], rtol=1e-8)
+
+
+def test_bitwise_determinism(handle):
+    s = W.diffusion27(16, seed=2)
+    rows, cols, vals = s.coo()
+    a = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 20000, 1e-10)
+    b = handle.coo_solve(s.n, None, None, None, s.diag, s.b, 20000, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    assert a.status == b.status == X.SUCCESS
+    assert a.iters == b.iters and np.array_equal(a.x, b.x)
+
+
+def test_example_known_answer(handle):
+    """The reference example's three solves (pcg/sw/examples/c/example.c)."""
+    n = 65536
+    (r, c, d), (ri, cp, cd), diag, b1, b2, b3 = W.example_tridiagonal(n)
+    res1 = handle.coo_solve(n, r, c, d, diag, b1, 100, 1e-16)
+    assert res1.status == X.SUCCESS, res1.message
+    rp, ci, pm = oracle.coo_to_csr(n, r, c)
+    ref1 = oracle.jpcg(rp, ci, d[pm], diag, b1, 100, 1e-16)
+    assert abs(res1.iters - ref1["iters"]) <= 1
+    assert np.linalg.norm(res1.x - ref1["x"]) / np.linalg.norm(ref1["x"]) <= X_TOL
+    res2 = handle.coo_solve(n, None, None, d, diag, b2, 100, 1e-16, mode=X.MODE_KEEP_NZ_LAYOUT)
+    assert res2.status == X.SUCCESS, res2.message
+    ref2 = oracle.jpcg(rp, ci, d[pm], diag, b2, 100, 1e-16)
+    assert np.linalg.norm(res2.x - ref2["x"]) / np.linalg.norm(ref2["x"]) <= X_TOL
+    res3 = handle.csc_sym_solve(n, ri, cp, cd, diag, b3, 100, 1e-16,
+                                mode=X.MODE_DEFAULT | X.MODE_FORTRAN_INDEX)
+    assert res3.status == X.SUCCESS, res3.message
+    ref3 = oracle.jpcg(rp, ci, d[pm], diag, b3, 100, 1e-16)
+    assert abs(res3.iters - ref3["iters"]) <= 1
+    assert np.linalg.norm(res3.x - ref3["x"]) / np.linalg.norm(ref3["x"]) <= X_TOL
+
+
+def test_host_loop_matches_graph_loop(gpu_lib):
+    s = W.poisson7(16)
+    rows, cols, vals = s.coo()
+    with X.JPCG() as h:
+        a = h.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 2000, 1e-10)
+        assert h.info().loopMode == 1
+    os.environ["XJPCG_HOST_LOOP"] = "1"
+    try:
+        with X.JPCG() as h:
+            b = h.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 2000, 1e-10)
+            assert h.info().loopMode == 0
+    finally:
+        del os.environ["XJPCG_HOST_LOOP"]
+    assert a.iters == b.iters and np.array_equal(a.x, b.x)
+
+
+def test_zero_rhs_breakdown(handle):
+    s = W.poisson7(8)
+    rows, cols, vals = s.coo()
+    r = handle.coo_solve(s.n, rows, cols, vals, s.diag, np.zeros(s.n), 50, 1e-10)
+    # b = 0 makes alpha = 0/0; the loop stops at that iteration instead of
+    # running to maxIter on NaN.
+    assert r.status == X.EXECUTION_FAILED
+    assert handle.info().itersRun == 1
+
+
+def test_mixed_precision_small(handle):
+    s = W.zipf_spd(20000, seed=2)
+    r64 = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
+    assert r64.status == X.SUCCESS, r64.message
+    m = handle.mixed_solve(s.b, s.diag, 20000, 1e-10)
+    assert m.status == X.SUCCESS, m.message
+    rel = oracle.true_relres(s.rowptr, s.col, s.val, s.b, m.x)
+    assert rel <= 1e-10 * 1.5, rel
+    tight = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 200000, 1e-14)
+    err = np.linalg.norm(m.x - tight["x"]) / np.linalg.norm(tight["x"])
+    err64 = np.linalg.norm(r64.x - tight["x"]) / np.linalg.norm(tight["x"])
+    assert err <= max(10 * err64, 1e-8), (err, err64)
+    assert handle.info().outerSweeps >= 1
