@@ -231,6 +231,7 @@ def run_gb300(args):
 
     r0 = e2e_step()  # sets the matrix, tunes the SpMV
     info = h.info()
+    tuning = h.spmv_tuning()
     d_b = torch.from_numpy(sysm.b).cuda()
     d_diag = torch.from_numpy(sysm.diag).cuda()
     d_x = torch.zeros(n, dtype=torch.float64, device="cuda")
@@ -315,7 +316,8 @@ def run_gb300(args):
                 "warmup": max(args.warmup, 3), "ms_per_step": ttt * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single",
-                               spmv_lanes=info.spmvLanes, spmv_grid=info.spmvGrid),
+                               spmv_lanes=info.spmvLanes, spmv_grid=info.spmvGrid,
+                               spmv_tuning=[list(t) for t in tuning]),
                 "time_to_tol_s": ttt, "iters": k_iters, "iter_ms": iter_ms, "iter_gbs": iter_gbs,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,

@@ -36,6 +36,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_cooSolver", "xJPCG_peekAtLastStatus", "xJPCG_getLastMessage", "xJPCG_getMetrics",
     "xJPCG_gbCsrSolver", "xJPCG_gbSolveDevice", "xJPCG_gbMixedSolve", "xJPCG_gbSpmv", "xJPCG_gbGetCsr",
     "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes",
+    "xJPCG_gbGetSpmvTuning",
 ]
 
 
@@ -102,6 +103,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbGetInfo.argtypes = [_P, C.POINTER(GbInfo)]
     lib.xJPCG_gbGetStream.argtypes = [_P, C.POINTER(_P)]
     lib.xJPCG_gbSetSpmvLanes.argtypes = [_P, C.c_int]
+    lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
         if name not in ("xJPCG_getErrorString", "xJPCG_getLastMessage"):
@@ -189,7 +191,8 @@ class JPCG:
                   x: Optional[np.ndarray] = None) -> SolveResult:
         x = np.zeros(n, np.float64) if x is None else x
         it, res = C.c_uint32(0), C.c_double(0.0)
-        nnz = len(data) if nnz is None else nnz
+        if nnz is None:
+            nnz = len(data) if data is not None else (len(row) if row is not None else 0)
         st = self.lib.xJPCG_cooSolver(self.h, n, nnz, _ptr(row), _ptr(col), _ptr(data), _ptr(diag), _ptr(b), _ptr(x),
                                       max_iter, tol, C.byref(it), C.byref(res), mode)
         return SolveResult(st, x, it.value, res.value, self.last_message())
@@ -198,7 +201,8 @@ class JPCG:
                       x: Optional[np.ndarray] = None) -> SolveResult:
         x = np.zeros(n, np.float64) if x is None else x
         it, res = C.c_int64(0), C.c_double(0.0)
-        nnz = len(data) if nnz is None else nnz
+        if nnz is None:
+            nnz = len(data) if data is not None else (len(row_idx) if row_idx is not None else 0)
         st = self.lib.xJPCG_cscSymSolver(self.h, n, nnz, _ptr(row_idx), _ptr(col_ptr), _ptr(data), _ptr(diag),
                                          _ptr(b), _ptr(x), max_iter, tol, C.byref(it), C.byref(res), mode)
         return SolveResult(st, x, it.value, res.value, self.last_message())
@@ -253,6 +257,14 @@ class JPCG:
         if st != SUCCESS:
             raise XJPCGError(st, self.last_message())
         return buf[:cnt.value]
+
+    def spmv_tuning(self):
+        """[(lanes, consumers, chunk, stages, ms)] of the last SpMV tuning."""
+        ms = np.zeros(64, np.float32)
+        shape = np.zeros(256, np.int32)
+        cnt = C.c_int32(0)
+        self.lib.xJPCG_gbGetSpmvTuning(self.h, _ptr(ms), _ptr(shape), 64, C.byref(cnt))
+        return [tuple(int(v) for v in shape[4 * i:4 * i + 4]) + (float(ms[i]),) for i in range(cnt.value)]
 
     def set_spmv_lanes(self, lanes: int):
         st = self.lib.xJPCG_gbSetSpmvLanes(self.h, lanes)

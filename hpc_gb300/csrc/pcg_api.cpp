@@ -329,6 +329,14 @@ XJPCG_Status_t xJPCG_gbGetInfo(const XJPCG_Handle_t* handle, XJPCG_GbInfo_t* inf
     return XJPCG_STATUS_SUCCESS;
 }
 
+XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, int32_t* shape, int32_t cap,
+                                     int32_t* count) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    if (ms == nullptr || shape == nullptr || count == nullptr) return XJPCG_STATUS_INVALID_VALUE;
+    *count = impl(handle)->tuning(ms, shape, cap);
+    return XJPCG_STATUS_SUCCESS;
+}
+
 XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream) {
     if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
     if (stream == nullptr) return XJPCG_STATUS_INVALID_VALUE;

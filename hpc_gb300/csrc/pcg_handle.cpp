@@ -88,7 +88,7 @@ void PcgHandle::setCooMat(uint32_t n, uint64_t nnz, const uint32_t* row, const u
     check(cudaMemcpyAsync(m_inCol.p, col, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D cols");
     check(cudaMemcpyAsync(m_inVal.p, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D values");
     const uint64_t nnzPad = (nnz + 3) / 4 * 4 + 4;
-    alloc(m_rowptr, sizeof(int) * ((size_t)n + 1), "CSR row pointers");
+    alloc(m_rowptr, sizeof(int) * ((size_t)n + 1 + kRowptrPad), "CSR row pointers");
     alloc(m_col, sizeof(int) * nnzPad, "CSR columns");
     alloc(m_val, sizeof(double) * nnzPad, "CSR values");
     alloc(m_perm, sizeof(uint32_t) * (nnz + 1), "CSR permutation");
@@ -182,7 +182,7 @@ void PcgHandle::setCscSymMat(uint32_t n, uint64_t nnzHalf, const int64_t* rowIdx
     std::vector<uint32_t> dummy;
     const uint64_t nnz = nnzFull;
     const uint64_t nnzPad = (nnz + 3) / 4 * 4 + 4;
-    alloc(m_rowptr, sizeof(int) * ((size_t)n + 1), "CSR row pointers");
+    alloc(m_rowptr, sizeof(int) * ((size_t)n + 1 + kRowptrPad), "CSR row pointers");
     alloc(m_col, sizeof(int) * nnzPad, "CSR columns");
     alloc(m_val, sizeof(double) * nnzPad, "CSR values");
     alloc(m_perm, sizeof(uint32_t) * (nnz + 1), "CSR permutation");
@@ -248,6 +248,7 @@ void PcgHandle::finishMatrix() {
     const uint64_t nnzPad = (m_nnz + 3) / 4 * 4 + 4;
     check(cudaMemsetAsync(m_val.as<double>() + m_nnz, 0, sizeof(double) * (nnzPad - m_nnz), m_stream), "memset");
     check(cudaMemsetAsync(m_col.as<int>() + m_nnz, 0, sizeof(int) * (nnzPad - m_nnz), m_stream), "memset");
+    check(cudaMemsetAsync(m_rowptr.as<int>() + m_n + 1, 0, sizeof(int) * kRowptrPad, m_stream), "memset");
     m_val32Valid = false;
     check(cudaStreamSynchronize(m_stream), "sync");
     m_haveMatrix = true;
@@ -271,6 +272,7 @@ void PcgHandle::tuneSpmv() {
             if (spmv_config_lanes(c) == m_forcedLanes) best = c;
         if (best < 0) throw InvalidValue("unsupported SpMV lanes per row.");
     } else {
+        m_tuneMs.assign(ncfg, -1.f);
         check(cudaMemsetAsync(m_p.p, 0, sizeof(double) * m_n4, m_stream), "memset");
         for (int c = 0; c < ncfg; ++c) {
             const int grid = spmv_grid<double>(c, (int)m_n, m_numSms);
@@ -287,6 +289,7 @@ void PcgHandle::tuneSpmv() {
                 if (rep > 0) check(cudaEventElapsedTime(&ms[rep - 1], m_ev0, m_ev1), "event");
             }
             std::sort(ms, ms + 3);
+            m_tuneMs[c] = ms[1];
             if (ms[1] < bestMs) {
                 bestMs = ms[1];
                 best = c;
@@ -646,6 +649,15 @@ uint64_t PcgHandle::getRecords(void* buf, uint64_t cap) {
     check(cudaMemcpyAsync(buf, m_records.p, sizeof(IterRecord) * cnt, cudaMemcpyDeviceToHost, m_stream), "D2H");
     check(cudaStreamSynchronize(m_stream), "sync");
     return cnt;
+}
+
+int PcgHandle::tuning(float* ms, int* shape, int cap) const {
+    const int ncfg = spmv_num_configs();
+    for (int c = 0; c < ncfg && c < cap; ++c) {
+        ms[c] = c < (int)m_tuneMs.size() ? m_tuneMs[c] : -1.f;
+        spmv_config_shape(c, &shape[4 * c], &shape[4 * c + 1], &shape[4 * c + 2], &shape[4 * c + 3]);
+    }
+    return ncfg;
 }
 
 void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {

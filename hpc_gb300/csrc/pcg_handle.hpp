@@ -87,6 +87,7 @@ class PcgHandle {
     void getCsr(int32_t* rowPtr, int32_t* colIdx, double* values, uint32_t* perm);
     uint64_t getRecords(void* buf, uint64_t cap);
     void fillInfo(XJPCG_GbInfo_t* info) const;
+    int tuning(float* ms, int* shape, int cap) const;
     void setLanes(int lanes);
 
     bool hasMatrix() const { return m_haveMatrix; }
@@ -141,6 +142,7 @@ class PcgHandle {
     int m_spmvCfg = 2;
     int m_spmvGrid32Cfg = 2;
     int m_spmvGrid = 0;
+    std::vector<float> m_tuneMs;  // median time of each SpMV configuration at the last tuning
 
     // vectors
     uint32_t m_vecN = 0, m_n4 = 0;

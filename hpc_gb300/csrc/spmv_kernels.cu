@@ -1,24 +1,40 @@
 // spmv_kernels.cu -- CSR SpMV for sm_103a.
 //
-// One persistent kernel family, templated on the value type, the threads per
-// CTA (NT), the lanes per row (G), the nnz chunk size (C) and the pipeline
-// depth (S).  Rows are cut into tiles of R = NT/G consecutive rows; a CTA walks
-// its tiles (blockIdx.x, +gridDim.x, ...) and streams each tile's nnz range
-// [rowptr[r0], rowptr[r0+R]) through shared memory in chunks of C values and C
-// column indices.  Chunks are moved by cp.async.bulk (TMA bulk copies, no
-// tensor map needed for 1-D ranges) that complete on per-stage mbarriers, with
-// an L2 evict-first policy so the streamed matrix does not push the gathered
-// vector out of L2.  Thread 0 keeps S chunks in flight ahead of the consumers.
-// A row's G lanes stride over its entries in each chunk and keep their partial
-// sum in registers across chunks, so rows of any length are handled; the G
-// partials are combined with a fixed shuffle tree at the end of the tile.
+// A persistent, warp-specialized kernel family, templated on the value type,
+// the consumer threads per CTA (NC), the lanes per row (G), the nnz chunk size
+// (C) and the pipeline depth (S).  Rows are cut into tiles of R = NC/G
+// consecutive rows; CTA b walks tiles b, b+gridDim.x, ...  A tile's nnz range
+// [rowptr[r0], rowptr[r0+R]) is streamed through shared memory in chunks of at
+// most C entries ("jobs").
+//
+//   warp 0 (producer)   one lane reads the tile bounds from global memory and,
+//                       per job, issues three cp.async.bulk copies (TMA bulk
+//                       copies of 1-D ranges): the tile's row-pointer slice,
+//                       the chunk's values and its column indices, completing
+//                       on the stage's "full" mbarrier.  The matrix is read
+//                       with an L2 evict-first policy so the gathered vector
+//                       stays resident in L2.  Before reusing a stage the lane
+//                       waits on its "empty" mbarrier.
+//   warps 1.. (consumers)
+//                       G lanes per row stride over the row's entries of the
+//                       chunk (two independent FP64 accumulators per lane),
+//                       gather x through the read-only path, and release the
+//                       stage with one arrive per warp.  Partial sums stay in
+//                       registers across the chunks of a tile, so rows of any
+//                       length are handled; the G partials are combined with
+//                       a fixed shuffle tree when the tile ends.
+//
+// Consumers read nothing from global memory but x (and p / b for the fused
+// epilogues), so the only latency they see is the gather's.  Every wait is
+// bounded in time; on a timeout the CTA records kStatusWaitTimeout, drains its
+// copies in flight and leaves, and the solver loop stops.
 //
 // Modes (runtime, uniform across the grid):
 //   kPlain     y = A x
 //   kCgDot     y = A p, then p.y reduced over the grid; the last CTA writes
 //              pAp and alpha = rz / pAp into the solver state.  This is the
 //              reference's SpMV chain plus krnl_storeApk (pcg/hw/src/
-//              krnl_storeApk.cpp:63-73) fused into one launch.
+//              krnl_storeApk.cpp:63-73) in one launch.
 //   kResidual  y = b - A x and ||y||^2 reduced into state->rrTrue (true
 //              residual of the mixed-precision refinement loop).
 #include <algorithm>
@@ -42,143 +58,156 @@ struct AccOf<float> {
 
 constexpr uint64_t kWaitBudgetNs = 2000000000ull;  // 2 s per wait, far above any chunk
 
-template <typename VT, int NT, int G, int C, int S>
-__global__ void __launch_bounds__(NT) spmv_staged_kernel(int n, int ntiles, const int* __restrict__ rowptr,
-                                                         const int* __restrict__ col, const VT* __restrict__ val,
-                                                         const VT* __restrict__ x, VT* __restrict__ y,
-                                                         const VT* __restrict__ b, CgState* state,
-                                                         double* partials, int mode, const uint32_t* doneFlag) {
-    typedef typename AccOf<VT>::type AccT;
-    constexpr int R = NT / G;
-    constexpr int CP = C + 4;  // stage capacity: a chunk widened to 4-element alignment
-    static_assert(NT % 32 == 0 && 32 % G == 0, "bad shape");
-    static_assert((CP * sizeof(VT)) % 16 == 0 && (CP * 4) % 16 == 0, "stage alignment");
+template <typename VT, int NC, int G, int C, int S>
+struct SpmvShape {
+    static constexpr int NT = NC + 32;  // + producer warp
+    static constexpr int R = NC / G;    // rows per tile
+    static constexpr int RP = R + 4;    // row-pointer slice, padded to 16 bytes
+    static constexpr int CP = C + 4;    // chunk capacity widened to 4-entry alignment
+    static constexpr size_t kValOff = 0;
+    static constexpr size_t kColOff = kValOff + sizeof(VT) * (size_t)S * CP;
+    static constexpr size_t kRpOff = kColOff + sizeof(int) * (size_t)S * CP;
+    static constexpr size_t kSmem = kRpOff + sizeof(int) * (size_t)S * RP;
+    static_assert(NC % 32 == 0 && 32 % G == 0 && R % 4 == 0, "bad shape");
+    static_assert((CP * sizeof(VT)) % 16 == 0 && (CP * 4) % 16 == 0 && (RP * 4) % 16 == 0, "stage alignment");
+};
 
+template <typename VT, int NC, int G, int C, int S>
+__global__ void __launch_bounds__(NC + 32) spmv_ws_kernel(int n, int ntiles, const int* __restrict__ rowptr,
+                                                          const int* __restrict__ col, const VT* __restrict__ val,
+                                                          const VT* __restrict__ x, VT* __restrict__ y,
+                                                          const VT* __restrict__ b, CgState* state,
+                                                          double* partials, int mode, const uint32_t* doneFlag) {
+    typedef SpmvShape<VT, NC, G, C, S> Sh;
+    typedef typename AccOf<VT>::type AccT;
+    constexpr int R = Sh::R;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    VT* sval = reinterpret_cast<VT*>(smem_raw);
-    int* scol = reinterpret_cast<int*>(smem_raw + sizeof(VT) * S * CP);
+    VT* sval = reinterpret_cast<VT*>(smem_raw + Sh::kValOff);
+    int* scol = reinterpret_cast<int*>(smem_raw + Sh::kColOff);
+    int* srp = reinterpret_cast<int*>(smem_raw + Sh::kRpOff);
     __shared__ __align__(8) uint64_t fullBar[S];
-    __shared__ int abortFlag;
+    __shared__ __align__(8) uint64_t emptyBar[S];
+    __shared__ volatile int abortFlag;
 
     if (doneFlag && *(volatile const uint32_t*)doneFlag) return;
 
     const int tid = threadIdx.x;
-    const int lane = tid % G;
-    const int grp = tid / G;
-
-    // ---- producer state (thread 0 only) ----
-    int pTile = (int)blockIdx.x - (int)gridDim.x, pChunk = 0, pNch = 0, pTs = 0, pTe = 0;
-    bool pHas = true;
-    uint64_t pol = 0;
-    auto pAdvance = [&]() -> bool {
-        ++pChunk;
-        while (pChunk >= pNch) {
-            pTile += gridDim.x;
-            if (pTile >= ntiles) return false;
-            const int r0 = pTile * R, r1 = min(r0 + R, n);
-            pTs = rowptr[r0];
-            pTe = rowptr[r1];
-            pNch = (pTe - pTs + C - 1) / C;
-            pChunk = 0;
-        }
-        return true;
-    };
-    auto pIssue = [&](int job) {
-        const int cs = pTs + pChunk * C;
-        const int ce = min(cs + C, pTe);
-        const int a0 = cs & ~3, a1 = (ce + 3) & ~3;
-        const uint32_t cnt = (uint32_t)(a1 - a0);
-        const int st = job % S;
-        mbar_arrive_expect_tx(&fullBar[st], cnt * (uint32_t)(sizeof(VT) + 4));
-        bulk_g2s(sval + st * CP, val + a0, cnt * (uint32_t)sizeof(VT), &fullBar[st], pol);
-        bulk_g2s(scol + st * CP, col + a0, cnt * 4u, &fullBar[st], pol);
-    };
-
+    const int warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         abortFlag = 0;
 #pragma unroll
-        for (int s = 0; s < S; ++s) mbar_init(&fullBar[s], 1);
+        for (int s = 0; s < S; ++s) {
+            mbar_init(&fullBar[s], 1);
+            mbar_init(&emptyBar[s], NC / 32);
+        }
         mbar_fence_init();
     }
     __syncthreads();
-    int issued = 0;
-    if (tid == 0) {
-        pol = l2_policy_evict_first();
-        for (int s = 0; s < S; ++s) {
-            pHas = pAdvance();
-            if (!pHas) break;
-            pIssue(s);
-            ++issued;
-        }
-    }
 
     AccT dacc = AccT(0);
-    int job = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int r0 = t * R, r1 = min(r0 + R, n);
-        const int ts = rowptr[r0], te = rowptr[r1];
-        const int row = r0 + grp;
-        int rs = 0, re = 0;
-        if (row < r1) {
-            rs = rowptr[row];
-            re = rowptr[row + 1];
-        }
-        AccT acc = AccT(0);
-        const int nch = (te - ts + C - 1) / C;
-        for (int c = 0; c < nch; ++c, ++job) {
-            const int st = job % S;
-            const uint32_t parity = (uint32_t)(job / S) & 1u;
-            if (!mbar_wait_bounded(&fullBar[st], parity, kWaitBudgetNs)) abortFlag = 1;
-            const int cs = ts + c * C;
-            const int ce = min(cs + C, te);
-            const int base = st * CP - (cs & ~3);
-            const int lo = max(rs, cs), hi = min(re, ce);
-#pragma unroll 4
-            for (int e = lo + lane; e < hi; e += G) {
-                const VT v = sval[base + e];
-                const int cidx = scol[base + e];
-                acc = fma((AccT)v, (AccT)__ldg(&x[cidx]), acc);
+    if (warp == 0) {
+        // ------------------------------ producer ------------------------------
+        if (lane == 0) {
+            const uint64_t pol = l2_policy_evict_first();
+            int job = 0;
+            for (int t = blockIdx.x; t < ntiles && !abortFlag; t += gridDim.x) {
+                const int r0 = t * R, r1 = min(r0 + R, n);
+                const int ts = __ldg(&rowptr[r0]), te = __ldg(&rowptr[r1]);
+                const int nch = max(1, (te - ts + C - 1) / C);
+                for (int c = 0; c < nch; ++c, ++job) {
+                    const int st = job % S;
+                    if (!mbar_wait_bounded(&emptyBar[st], ((uint32_t)(job / S) & 1u) ^ 1u, kWaitBudgetNs)) {
+                        abortFlag = 1;
+                        break;
+                    }
+                    const int cs = ts + c * C, ce = min(cs + C, te);
+                    const int a0 = cs & ~3, a1 = (ce + 3) & ~3;
+                    const uint32_t cnt = ce > cs ? (uint32_t)(a1 - a0) : 0u;
+                    mbar_arrive_expect_tx(&fullBar[st], (uint32_t)Sh::RP * 4u + cnt * (uint32_t)(sizeof(VT) + 4));
+                    bulk_g2s(srp + st * Sh::RP, rowptr + r0, (uint32_t)Sh::RP * 4u, &fullBar[st], pol);
+                    if (cnt) {
+                        bulk_g2s(sval + st * Sh::CP, val + a0, cnt * (uint32_t)sizeof(VT), &fullBar[st], pol);
+                        bulk_g2s(scol + st * Sh::CP, col + a0, cnt * 4u, &fullBar[st], pol);
+                    }
+                }
             }
-            __syncthreads();
+            if (abortFlag) {
+                // Drain: the last S jobs may still be in flight.
+                for (int j = max(0, job - S); j < job; ++j)
+                    mbar_wait_bounded(&fullBar[j % S], (uint32_t)(j / S) & 1u, kWaitBudgetNs);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------ consumers -----------------------------
+        const int ctid = tid - 32;
+        const int lg = ctid % G;
+        const int grp = ctid / G;
+        int job = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            const int r0 = t * R, r1 = min(r0 + R, n);
+            const int row = r0 + grp;
+            const bool live = row < r1;
+            AccT pRow = AccT(0);
+            if (mode == kCgDot && lg == 0 && live) pRow = (AccT)__ldg(&x[row]);
+            if (mode == kResidual && lg == 0 && live) pRow = (AccT)__ldg(&b[row]);
+            AccT a0 = AccT(0), a1 = AccT(0);
+            int nch = 1;
+            for (int c = 0; c < nch; ++c, ++job) {
+                const int st = job % S;
+                if (!mbar_wait_bounded(&fullBar[st], (uint32_t)(job / S) & 1u, kWaitBudgetNs)) abortFlag = 1;
+                if (abortFlag) break;
+                const int* rp = srp + st * Sh::RP;
+                const int ts = rp[0], te = rp[r1 - r0];
+                nch = max(1, (te - ts + C - 1) / C);
+                const int cs = ts + c * C, ce = min(cs + C, te);
+                const int base = st * Sh::CP - (cs & ~3);
+                int lo = cs, hi = cs;
+                if (live) {
+                    lo = max(rp[grp], cs);
+                    hi = min(rp[grp + 1], ce);
+                }
+                int e = lo + lg;
+#pragma unroll 2
+                for (; e + G < hi; e += 2 * G) {
+                    const VT v0 = sval[base + e], v1 = sval[base + e + G];
+                    const int c0 = scol[base + e], c1 = scol[base + e + G];
+                    a0 = fma((AccT)v0, (AccT)__ldg(&x[c0]), a0);
+                    a1 = fma((AccT)v1, (AccT)__ldg(&x[c1]), a1);
+                }
+                if (e < hi) a0 = fma((AccT)sval[base + e], (AccT)__ldg(&x[scol[base + e]]), a0);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&emptyBar[st]);
+            }
             if (abortFlag) break;
-            if (tid == 0 && pHas) {
-                pHas = pAdvance();
-                if (pHas) {
-                    pIssue(job + S);
-                    ++issued;
+            AccT acc = a0 + a1;
+            if (G > 1) {
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            }
+            if (lg == 0 && live) {
+                if (mode == kResidual) {
+                    const AccT rv = pRow - acc;
+                    y[row] = (VT)rv;
+                    dacc = fma(rv, rv, dacc);
+                } else {
+                    y[row] = (VT)acc;
+                    if (mode == kCgDot) dacc = fma(pRow, acc, dacc);
                 }
             }
         }
-        if (abortFlag) break;
-        if (G > 1) {
-#pragma unroll
-            for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        }
-        if (lane == 0 && row < r1) {
-            if (mode == kResidual) {
-                const AccT rv = (AccT)b[row] - acc;
-                y[row] = (VT)rv;
-                dacc = fma(rv, rv, dacc);
-            } else {
-                y[row] = (VT)acc;
-                if (mode == kCgDot) dacc = fma((AccT)x[row], acc, dacc);
-            }
-        }
     }
-
+    __syncthreads();
     if (abortFlag) {
-        // Drain copies still in flight so no bulk write lands after exit.
         if (tid == 0) {
-            for (int j = job; j < issued; ++j) mbar_wait_bounded(&fullBar[j % S], (uint32_t)(j / S) & 1u, kWaitBudgetNs);
             atomicOr(&state->status, kStatusWaitTimeout);
             *(volatile uint32_t*)&state->done = 1u;  // later kernels of the loop stand down
         }
         return;
     }
-
     if (mode == kPlain) return;
     AccT v[1] = {dacc};
-    block_sum<NT, 1, AccT>(v);
+    block_sum<Sh::NT, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
     if (grid_sum_last<1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
@@ -197,61 +226,52 @@ __global__ void __launch_bounds__(NT) spmv_staged_kernel(int n, int ntiles, cons
 // ---------------------------------------------------------------------------
 namespace {
 
-template <typename VT, int NT, int G, int C, int S>
+template <typename VT, int NC, int G, int C, int S>
 struct SpmvInst {
-    static constexpr size_t smem() { return (size_t)S * (C + 4) * (sizeof(VT) + 4); }
+    typedef SpmvShape<VT, NC, G, C, S> Sh;
     static cudaError_t setup() {
-        return cudaFuncSetAttribute(spmv_staged_kernel<VT, NT, G, C, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem());
+        return cudaFuncSetAttribute(spmv_ws_kernel<VT, NC, G, C, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)Sh::kSmem);
     }
     static int blocksPerSm() {
         int nb = 0;
         if (setup() != cudaSuccess) return 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_staged_kernel<VT, NT, G, C, S>, NT, smem()) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_ws_kernel<VT, NC, G, C, S>, Sh::NT, Sh::kSmem) !=
             cudaSuccess)
             return 0;
         return nb;
     }
     static cudaError_t launch(int grid, cudaStream_t st, int n, const int* rp, const int* ci, const VT* v, const VT* x,
-                              VT* y, const VT* b, CgState* state, double* partials, int mode, const uint32_t* doneFlag) {
-        const int ntiles = (n + NT / G - 1) / (NT / G);
-        spmv_staged_kernel<VT, NT, G, C, S>
-            <<<grid, NT, smem(), st>>>(n, ntiles, rp, ci, v, x, y, b, state, partials, mode, doneFlag);
+                              VT* y, const VT* b, CgState* state, double* partials, int mode,
+                              const uint32_t* doneFlag) {
+        const int ntiles = (n + Sh::R - 1) / Sh::R;
+        spmv_ws_kernel<VT, NC, G, C, S>
+            <<<grid, Sh::NT, Sh::kSmem, st>>>(n, ntiles, rp, ci, v, x, y, b, state, partials, mode, doneFlag);
         return cudaGetLastError();
     }
-    static int tiles(int n) { return (n + NT / G - 1) / (NT / G); }
+    static int tiles(int n) { return (n + Sh::R - 1) / Sh::R; }
 };
 
 template <typename VT>
-struct Table;
-
-#define XJPCG_SPMV_ROWS(VT)                                                                              \
-    {1, &SpmvInst<VT, 256, 1, 2048, 4>::blocksPerSm, &SpmvInst<VT, 256, 1, 2048, 4>::launch,          \
-     &SpmvInst<VT, 256, 1, 2048, 4>::tiles},                                                             \
-        {2, &SpmvInst<VT, 256, 2, 2048, 4>::blocksPerSm, &SpmvInst<VT, 256, 2, 2048, 4>::launch,      \
-         &SpmvInst<VT, 256, 2, 2048, 4>::tiles},                                                         \
-        {4, &SpmvInst<VT, 256, 4, 2048, 4>::blocksPerSm, &SpmvInst<VT, 256, 4, 2048, 4>::launch,      \
-         &SpmvInst<VT, 256, 4, 2048, 4>::tiles},                                                         \
-        {8, &SpmvInst<VT, 256, 8, 2048, 4>::blocksPerSm, &SpmvInst<VT, 256, 8, 2048, 4>::launch,      \
-         &SpmvInst<VT, 256, 8, 2048, 4>::tiles},                                                         \
-        {16, &SpmvInst<VT, 256, 16, 2048, 4>::blocksPerSm, &SpmvInst<VT, 256, 16, 2048, 4>::launch,   \
-         &SpmvInst<VT, 256, 16, 2048, 4>::tiles},                                                        \
-    {                                                                                                    \
-        32, &SpmvInst<VT, 256, 32, 2048, 4>::blocksPerSm, &SpmvInst<VT, 256, 32, 2048, 4>::launch,     \
-            &SpmvInst<VT, 256, 32, 2048, 4>::tiles                                                       \
-    }
-
-template <typename VT>
 struct Row {
-    int lanes;
+    int lanes, consumers, chunk, stages;
     int (*blocksPerSm)();
     cudaError_t (*launch)(int, cudaStream_t, int, const int*, const int*, const VT*, const VT*, VT*, const VT*,
                           CgState*, double*, int, const uint32_t*);
     int (*tiles)(int);
 };
 
-const Row<double> kRowsF64[] = {XJPCG_SPMV_ROWS(double)};
-const Row<float> kRowsF32[] = {XJPCG_SPMV_ROWS(float)};
+#define XJ_ROW(VT, NC, G, C, S) \
+    {G, NC, C, S, &SpmvInst<VT, NC, G, C, S>::blocksPerSm, &SpmvInst<VT, NC, G, C, S>::launch, \
+     &SpmvInst<VT, NC, G, C, S>::tiles}
+#define XJ_TABLE(VT)                                                                                     \
+    XJ_ROW(VT, 128, 1, 4096, 2), XJ_ROW(VT, 128, 2, 2048, 3), XJ_ROW(VT, 256, 2, 4096, 2),             \
+        XJ_ROW(VT, 256, 4, 2048, 4), XJ_ROW(VT, 128, 4, 1024, 4), XJ_ROW(VT, 256, 8, 2048, 4),          \
+        XJ_ROW(VT, 256, 16, 2048, 4), XJ_ROW(VT, 256, 32, 2048, 4)
+
+const Row<double> kRowsF64[] = {XJ_TABLE(double)};
+const Row<float> kRowsF32[] = {XJ_TABLE(float)};
+constexpr int kNumCfg = sizeof(kRowsF64) / sizeof(kRowsF64[0]);
 
 template <typename VT>
 const Row<VT>* rows();
@@ -266,8 +286,14 @@ const Row<float>* rows<float>() {
 
 }  // namespace
 
-int spmv_num_configs() { return 6; }
+int spmv_num_configs() { return kNumCfg; }
 int spmv_config_lanes(int cfg) { return kRowsF64[cfg].lanes; }
+void spmv_config_shape(int cfg, int* lanes, int* consumers, int* chunk, int* stages) {
+    *lanes = kRowsF64[cfg].lanes;
+    *consumers = kRowsF64[cfg].consumers;
+    *chunk = kRowsF64[cfg].chunk;
+    *stages = kRowsF64[cfg].stages;
+}
 
 template <typename VT>
 int spmv_grid(int cfg, int n, int numSms) {
@@ -280,7 +306,8 @@ int spmv_grid(int cfg, int n, int numSms) {
 
 template <typename VT>
 cudaError_t spmv_launch(int cfg, int grid, cudaStream_t st, int n, const int* rp, const int* ci, const VT* v,
-                        const VT* x, VT* y, const VT* b, CgState* state, double* partials, int mode, const uint32_t* doneFlag) {
+                        const VT* x, VT* y, const VT* b, CgState* state, double* partials, int mode,
+                        const uint32_t* doneFlag) {
     if (n <= 0) return cudaSuccess;
     return rows<VT>()[cfg].launch(grid, st, n, rp, ci, v, x, y, b, state, partials, mode, doneFlag);
 }
@@ -288,8 +315,10 @@ cudaError_t spmv_launch(int cfg, int grid, cudaStream_t st, int n, const int* rp
 template int spmv_grid<double>(int, int, int);
 template int spmv_grid<float>(int, int, int);
 template cudaError_t spmv_launch<double>(int, int, cudaStream_t, int, const int*, const int*, const double*,
-                                         const double*, double*, const double*, CgState*, double*, int, const uint32_t*);
+                                         const double*, double*, const double*, CgState*, double*, int,
+                                         const uint32_t*);
 template cudaError_t spmv_launch<float>(int, int, cudaStream_t, int, const int*, const int*, const float*,
-                                        const float*, float*, const float*, CgState*, double*, int, const uint32_t*);
+                                        const float*, float*, const float*, CgState*, double*, int,
+                                        const uint32_t*);
 
 }  // namespace xjpcg

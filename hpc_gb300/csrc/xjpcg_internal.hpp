@@ -10,6 +10,10 @@ struct CgState;
 // ---- SpMV (spmv_kernels.cu) ----
 int spmv_num_configs();
 int spmv_config_lanes(int cfg);
+void spmv_config_shape(int cfg, int* lanes, int* consumers, int* chunk, int* stages);
+// Row-pointer arrays must hold n + 1 + kRowptrPad entries (the SpMV copies
+// fixed-size, 16-byte aligned slices of them).
+constexpr int kRowptrPad = 160;
 template <typename VT>
 int spmv_grid(int cfg, int n, int numSms);
 template <typename VT>

@@ -75,6 +75,13 @@ XJPCG_Status_t xJPCG_gbGetRecords(XJPCG_Handle_t* handle, void* buf, uint64_t ca
 
 XJPCG_Status_t xJPCG_gbGetInfo(const XJPCG_Handle_t* handle, XJPCG_GbInfo_t* info);
 
+/* SpMV tuner report of the stored matrix: for each kernel configuration c
+ * (c < *count), ms[c] = median time of a plain SpMV (-1 if not timed) and
+ * shape[4c..4c+3] = lanes per row, consumer threads per CTA, chunk entries,
+ * pipeline stages.  At most cap configurations are written. */
+XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, int32_t* shape, int32_t cap,
+                                     int32_t* count);
+
 /* The cudaStream_t the handle launches on (for event timing by callers). */
 XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream);
 
