@@ -52,7 +52,7 @@ class GbInfo(C.Structure):
                 ("spmvLanes", C.c_uint32), ("spmvGrid", C.c_uint32), ("statusBits", C.c_uint32),
                 ("outerSweeps", C.c_uint32), ("innerIters", C.c_uint32), ("bb", C.c_double),
                 ("rrLast", C.c_double), ("solveMs", C.c_double), ("loopMode", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("spmvLayout", C.c_uint32)]
 
 
 RECORD_DTYPE = np.dtype([("id", "<u4"), ("iter", "<u4"), ("vecSize", "<u4"), ("maxIter", "<u4"),

@@ -126,6 +126,7 @@ void PcgHandle::updateCooValues(uint32_t n, uint64_t nnz, const double* data) {
     check(gather_values(m_stream, (int64_t)nnz, m_perm.as<uint32_t>(), m_inVal.as<double>(), m_val.as<double>()),
           "value gather");
     m_val32Valid = false;
+    refreshSellValues();
     check(cudaStreamSynchronize(m_stream), "sync");
 }
 
@@ -240,6 +241,7 @@ void PcgHandle::updateCscSymValues(uint32_t n, uint64_t nnzHalf, const int64_t* 
     check(gather_values(m_stream, (int64_t)nnzFull, m_perm.as<uint32_t>(), m_inVal.as<double>(), m_val.as<double>()),
           "value gather");
     m_val32Valid = false;
+    refreshSellValues();
     check(cudaStreamSynchronize(m_stream), "sync");
 }
 
@@ -250,6 +252,8 @@ void PcgHandle::finishMatrix() {
     check(cudaMemsetAsync(m_col.as<int>() + m_nnz, 0, sizeof(int) * (nnzPad - m_nnz), m_stream), "memset");
     check(cudaMemsetAsync(m_rowptr.as<int>() + m_n + 1, 0, sizeof(int) * kRowptrPad, m_stream), "memset");
     m_val32Valid = false;
+    m_sellState = 0;
+    m_sell32Valid = false;
     check(cudaStreamSynchronize(m_stream), "sync");
     m_haveMatrix = true;
     ensureVectors(m_n);
@@ -263,25 +267,98 @@ void PcgHandle::setLanes(int lanes) {
 
 // Picks the lanes-per-row shape by timing every SpMV configuration on the
 // stored matrix (plain mode, x = p buffer), median of three launches each.
+void PcgHandle::refreshSellValues() {
+    m_sell32Valid = false;
+    if (m_sellState != 1) return;
+    check(sell_fill<double>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                            m_sliceOff.as<int>(), nullptr, m_sellVal.as<double>()),
+          "sliced fill");
+}
+
+int PcgHandle::numSpmvCfgs() const { return spmv_num_configs() + sell_num_configs(); }
+
+bool PcgHandle::isSell(int cfg) const { return cfg >= spmv_num_configs(); }
+
+int PcgHandle::spmvGrid64(int cfg) {
+    if (!isSell(cfg)) return spmv_grid<double>(cfg, (int)m_n, m_numSms);
+    return ensureSell() ? sell_grid<double>(cfg - spmv_num_configs(), (int)m_n, m_numSms) : 0;
+}
+
+int PcgHandle::spmvGrid32(int cfg) {
+    if (!isSell(cfg)) return spmv_grid<float>(cfg, (int)m_n, m_numSms);
+    return sell_grid<float>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
+}
+
+cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, const double* b, CgState* st,
+                              double* part, int mode, const uint32_t* done) {
+    if (!isSell(cfg))
+        return spmv_launch<double>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
+                                   m_val.as<double>(), x, y, b, st, part, mode, done);
+    return spmv_sell_launch<double>(cfg - spmv_num_configs(), grid, m_stream, (int)m_n, m_sliceOff.as<int>(),
+                                    m_sellCol.as<int>(), m_sellVal.as<double>(), x, y, b, st, part, mode, done);
+}
+
+cudaError_t PcgHandle::spmv32(int cfg, int grid, const float* x, float* y, const float* b, CgState* st,
+                              double* part, int mode, const uint32_t* done) {
+    if (!isSell(cfg))
+        return spmv_launch<float>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
+                                  m_val32.as<float>(), x, y, b, st, part, mode, done);
+    return spmv_sell_launch<float>(cfg - spmv_num_configs(), grid, m_stream, (int)m_n, m_sliceOff.as<int>(),
+                                   m_sellCol.as<int>(), m_sellVal32.as<float>(), x, y, b, st, part, mode, done);
+}
+
+// Builds (once per matrix) the sliced copy used by the SELL kernels.  Returns
+// false when padding would exceed half the stored entries (irregular rows),
+// in which case the sliced configurations are not offered.
+bool PcgHandle::ensureSell() {
+    if (m_sellState == 1) return true;
+    if (m_sellState == 2) return false;
+    const int nslices = ((int)m_n + 31) / 32;
+    alloc(m_sliceOff, sizeof(int) * ((size_t)nslices + 1), "slice offsets");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count(nslices + 1) + 16), "scan scratch");
+    int64_t total = 0;
+    check(sell_build(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(), m_sliceOff.as<int>(),
+                     m_blockSums.as<int>(), &total),
+          "sliced layout");
+    if ((uint64_t)total > m_nnz + m_nnz / 2 + 64 || total > 0x7fffff00ll) {
+        m_sellState = 2;
+        return false;
+    }
+    alloc(m_sellCol, sizeof(int) * ((size_t)total + 32), "sliced columns");
+    alloc(m_sellVal, sizeof(double) * ((size_t)total + 32), "sliced values");
+    check(sell_fill<double>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                            m_sliceOff.as<int>(), m_sellCol.as<int>(), m_sellVal.as<double>()),
+          "sliced fill");
+    m_sellTotal = total;
+    m_sellState = 1;
+    m_sell32Valid = false;
+    return true;
+}
+
 void PcgHandle::tuneSpmv() {
-    const int ncfg = spmv_num_configs();
+    const int ncfg = numSpmvCfgs();
     int best = -1;
     float bestMs = 1e30f;
-    if (m_forcedLanes > 0) {
-        for (int c = 0; c < ncfg; ++c)
+    const int forcedCfg = envInt("XJPCG_SPMV_CFG", -1);
+    if (forcedCfg >= 0 && forcedCfg < ncfg) {
+        best = forcedCfg;
+    } else if (m_forcedLanes < 0) {
+        if (!ensureSell()) throw InvalidValue("the sliced SpMV layout is not available for this matrix.");
+        best = spmv_num_configs();
+    } else if (m_forcedLanes > 0) {
+        for (int c = spmv_num_configs() - 1; c >= 0; --c)
             if (spmv_config_lanes(c) == m_forcedLanes) best = c;
         if (best < 0) throw InvalidValue("unsupported SpMV lanes per row.");
     } else {
         m_tuneMs.assign(ncfg, -1.f);
         check(cudaMemsetAsync(m_p.p, 0, sizeof(double) * m_n4, m_stream), "memset");
         for (int c = 0; c < ncfg; ++c) {
-            const int grid = spmv_grid<double>(c, (int)m_n, m_numSms);
+            const int grid = spmvGrid64(c);
             if (grid <= 0) continue;
             float ms[3];
             for (int rep = 0; rep < 4; ++rep) {
                 check(cudaEventRecord(m_ev0, m_stream), "event");
-                check(spmv_launch<double>(c, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
-                                          m_val.as<double>(), m_p.as<double>(), m_Ap.as<double>(), nullptr,
+                check(spmv64(c, grid, m_p.as<double>(), m_Ap.as<double>(), nullptr,
                                           m_state.as<CgState>(), m_partials.as<double>(), kSpmvPlain, nullptr),
                       "SpMV");
                 check(cudaEventRecord(m_ev1, m_stream), "event");
@@ -298,7 +375,7 @@ void PcgHandle::tuneSpmv() {
         if (best < 0) throw InternalError("no SpMV configuration can be launched on this device.");
     }
     m_spmvCfg = best;
-    m_spmvGrid = spmv_grid<double>(best, (int)m_n, m_numSms);
+    m_spmvGrid = spmvGrid64(best);
     ++m_generation;  // graphs embed the configuration
 }
 
@@ -368,8 +445,7 @@ void PcgHandle::buildGraph() {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     check(cudaStreamBeginCaptureToGraph(m_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
           "capture body");
-    check(spmv_launch<double>(m_spmvCfg, m_spmvGrid, m_stream, n, m_rowptr.as<int>(), m_col.as<int>(),
-                              m_val.as<double>(), m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part, kSpmvCgDot,
+    check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part, kSpmvCgDot,
                               &st->done),
           "SpMV kernel");
     check(cg_update_launch(vg, m_stream, n4, m_x.as<double>(), m_r.as<double>(), m_p.as<double>(),
@@ -419,8 +495,7 @@ Results PcgHandle::run(uint32_t maxIter, double tol) {
         uint64_t ran = 0;
         for (;;) {
             for (int u = 0; u < 16; ++u) {
-                check(spmv_launch<double>(m_spmvCfg, m_spmvGrid, m_stream, n, m_rowptr.as<int>(), m_col.as<int>(),
-                                          m_val.as<double>(), m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part,
+                check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part,
                                           kSpmvCgDot, &st->done),
                       "SpMV kernel");
                 check(cg_update_launch(vg, m_stream, n4, m_x.as<double>(), m_r.as<double>(), m_p.as<double>(),
@@ -477,7 +552,7 @@ void PcgHandle::buildMixedGraph() {
     const int n = (int)m_n, n4 = (int)m_n4;
     const int vg = vec_grid(n4, m_numSms);
     const int cfg32 = m_spmvCfg;
-    const int grid32 = spmv_grid<float>(cfg32, n, m_numSms);
+    const int grid32 = spmvGrid32(cfg32);
     CgState* st = m_state.as<CgState>();
     CgState* in = m_state32.as<CgState>();
     double* part = m_partials.as<double>();
@@ -508,8 +583,7 @@ void PcgHandle::buildMixedGraph() {
     check(cudaGraphConditionalHandleCreate(&m_condInner, outerBody, 0, 0), "handle");
     check(cudaStreamBeginCaptureToGraph(m_stream, outerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
           "capture");
-    check(spmv_launch<double>(m_spmvCfg, m_spmvGrid, m_stream, n, m_rowptr.as<int>(), m_col.as<int>(),
-                              m_val.as<double>(), m_x.as<double>(), m_r.as<double>(), m_b.as<double>(), st, part,
+    check(spmv64(m_spmvCfg, m_spmvGrid, m_x.as<double>(), m_r.as<double>(), m_b.as<double>(), st, part,
                               kSpmvResidual, nullptr),
           "residual SpMV");
     check(ir_check_launch(m_stream, st, in, (uint64_t)m_condOuter, kMaxOuter), "ir check");
@@ -539,8 +613,7 @@ void PcgHandle::buildMixedGraph() {
     cudaGraph_t innerBody = ip.conditional.phGraph_out[0];
     check(cudaStreamBeginCaptureToGraph(m_stream, innerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
           "capture");
-    check(spmv_launch<float>(cfg32, grid32, m_stream, n, m_rowptr.as<int>(), m_col.as<int>(), m_val32.as<float>(),
-                             m_p32.as<float>(), m_Ap32.as<float>(), nullptr, in, part, kSpmvCgDot, &in->done),
+    check(spmv32(cfg32, grid32, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, in, part, kSpmvCgDot, &in->done),
           "SpMV fp32");
     check(cg32_update_launch(vg, m_stream, n4, m_d32.as<float>(), m_r32.as<float>(), m_p32.as<float>(),
                              m_Ap32.as<float>(), m_J32.as<float>(), in, part, (uint64_t)m_condInner, 1),
@@ -571,6 +644,13 @@ Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
         alloc(m_val32, sizeof(float) * nnzPad, "fp32 values");
         check(convert_f64_to_f32(m_stream, (int64_t)nnzPad, m_val.as<double>(), m_val32.as<float>()), "fp32 values");
         m_val32Valid = true;
+    }
+    if (isSell(m_spmvCfg) && !m_sell32Valid) {
+        alloc(m_sellVal32, sizeof(float) * ((size_t)m_sellTotal + 32), "sliced fp32 values");
+        check(sell_fill<float>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                               m_sliceOff.as<int>(), nullptr, m_sellVal32.as<float>()),
+              "sliced fp32 fill");
+        m_sell32Valid = true;
     }
     check(cudaMemsetAsync(m_p32.p, 0, vb32, m_stream), "memset");
     check(cudaMemsetAsync(m_Ap32.p, 0, vb32, m_stream), "memset");
@@ -620,8 +700,7 @@ void PcgHandle::spmv(const double* x, double* y, bool onDevice) {
         dx = m_b.as<double>();
         dy = m_scratchY.as<double>();
     }
-    check(spmv_launch<double>(m_spmvCfg, m_spmvGrid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
-                              m_val.as<double>(), dx, dy, nullptr, m_state.as<CgState>(), m_partials.as<double>(),
+    check(spmv64(m_spmvCfg, m_spmvGrid, dx, dy, nullptr, m_state.as<CgState>(), m_partials.as<double>(),
                               kSpmvPlain, nullptr),
           "SpMV");
     if (!onDevice) {
@@ -652,10 +731,18 @@ uint64_t PcgHandle::getRecords(void* buf, uint64_t cap) {
 }
 
 int PcgHandle::tuning(float* ms, int* shape, int cap) const {
-    const int ncfg = spmv_num_configs();
+    const int ncfg = numSpmvCfgs();
     for (int c = 0; c < ncfg && c < cap; ++c) {
         ms[c] = c < (int)m_tuneMs.size() ? m_tuneMs[c] : -1.f;
-        spmv_config_shape(c, &shape[4 * c], &shape[4 * c + 1], &shape[4 * c + 2], &shape[4 * c + 3]);
+        if (isSell(c)) {
+            // sliced layout: one lane per row, no CTA staging; chunk = unroll
+            shape[4 * c] = 1;
+            shape[4 * c + 1] = 0;
+            shape[4 * c + 2] = sell_config_unroll(c - spmv_num_configs());
+            shape[4 * c + 3] = 0;
+        } else {
+            spmv_config_shape(c, &shape[4 * c], &shape[4 * c + 1], &shape[4 * c + 2], &shape[4 * c + 3]);
+        }
     }
     return ncfg;
 }
@@ -666,7 +753,8 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->n4 = m_n4;
     info->nnz = m_nnz;
     info->itersRun = m_lastState.k;
-    info->spmvLanes = (uint32_t)spmv_config_lanes(m_spmvCfg);
+    info->spmvLanes = isSell(m_spmvCfg) ? 1u : (uint32_t)spmv_config_lanes(m_spmvCfg);
+    info->spmvLayout = isSell(m_spmvCfg) ? 1u : 0u;
     info->spmvGrid = (uint32_t)m_spmvGrid;
     info->statusBits = m_lastState.status;
     info->outerSweeps = m_lastOuter;

@@ -112,6 +112,16 @@ class PcgHandle {
     void alloc(DevBuf& b, size_t bytes, const char* what);
     void finishMatrix();     // after CSR exists: values pad, tuning
     void tuneSpmv();
+    int numSpmvCfgs() const;
+    bool isSell(int cfg) const;
+    int spmvGrid64(int cfg);
+    int spmvGrid32(int cfg);
+    bool ensureSell();
+    void refreshSellValues();
+    cudaError_t spmv64(int cfg, int grid, const double* x, double* y, const double* b, CgState* st, double* part,
+                       int mode, const uint32_t* done);
+    cudaError_t spmv32(int cfg, int grid, const float* x, float* y, const float* b, CgState* st, double* part,
+                       int mode, const uint32_t* done);
     void ensureVectors(uint32_t n);
     void buildGraph();
     void buildMixedGraph();
@@ -137,6 +147,11 @@ class PcgHandle {
     DevBuf m_rowptr, m_col, m_val, m_perm, m_val32;
     DevBuf m_inRow, m_inCol, m_inVal, m_inIdx64, m_inPtr64;
     DevBuf m_counts, m_fill, m_blockSums, m_keys, m_flags, m_cscScratch;
+    // sliced (SELL-32) copy of the matrix, built on demand by the tuner
+    DevBuf m_sliceOff, m_sellCol, m_sellVal, m_sellVal32;
+    int m_sellState = 0;  // 0 not built, 1 built, 2 rejected (too much padding)
+    int64_t m_sellTotal = 0;
+    bool m_sell32Valid = false;
     bool m_val32Valid = false;
     int m_forcedLanes = 0;
     int m_spmvCfg = 2;

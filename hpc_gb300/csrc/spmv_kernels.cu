@@ -322,3 +322,205 @@ template cudaError_t spmv_launch<float>(int, int, cudaStream_t, int, const int*,
                                         const uint32_t*);
 
 }  // namespace xjpcg
+
+// ===========================================================================
+// Sliced layout (SELL-32): rows in slices of 32, each slice padded to its
+// longest row and stored column-major (entry j of the slice's 32 rows is
+// contiguous).  One lane per row, no shared memory and no reduction: every
+// warp-wide load of values or columns is one contiguous 256-byte (values) or
+// 128-byte (columns) segment, occupancy is limited only by registers, and the
+// FP64 pipe sees exactly one DFMA per stored entry.  On this part FP64 issue
+// (about two DFMA per clock per SM) is as scarce as HBM bandwidth, so the
+// autotuner picks this layout for matrices with near-uniform row lengths
+// (stencils) and the staged CSR kernels above for irregular ones.  Padding
+// entries hold value 0 and the row's own index as column.
+// ===========================================================================
+namespace xjpcg {
+
+constexpr int kSellThreads = 256;
+
+__global__ void sell_slice_len_kernel(int n, const int* __restrict__ rowptr, int* __restrict__ sliceLen) {
+    const int lane = threadIdx.x & 31;
+    const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
+    const int nslices = (n + 31) / 32;
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warpsPerGrid) {
+        const int row = s * 32 + lane;
+        int len = row < n ? rowptr[row + 1] - rowptr[row] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+        if (lane == 0) sliceLen[s] = len * 32;
+    }
+}
+
+template <typename VT>
+__global__ void sell_fill_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                 const double* __restrict__ val, const int* __restrict__ sliceOff,
+                                 int* __restrict__ scol, VT* __restrict__ sval) {
+    const int lane = threadIdx.x & 31;
+    const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
+    const int nslices = (n + 31) / 32;
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warpsPerGrid) {
+        const int off = sliceOff[s];
+        const int len = (sliceOff[s + 1] - off) / 32;
+        const int row = s * 32 + lane;
+        const int rs = row < n ? rowptr[row] : 0;
+        const int rl = row < n ? rowptr[row + 1] - rs : 0;
+        for (int j = 0; j < len; ++j) {
+            const int dst = off + j * 32 + lane;
+            if (j < rl) {
+                if (scol) scol[dst] = col[rs + j];
+                sval[dst] = (VT)val[rs + j];
+            } else {
+                if (scol) scol[dst] = row < n ? row : 0;
+                sval[dst] = VT(0);
+            }
+        }
+    }
+}
+
+template <typename VT, int U>
+__global__ void __launch_bounds__(kSellThreads) spmv_sell_kernel(int n, int nslices, const int* __restrict__ sliceOff,
+                                                                 const int* __restrict__ scol,
+                                                                 const VT* __restrict__ sval, const VT* __restrict__ x,
+                                                                 VT* __restrict__ y, const VT* __restrict__ b,
+                                                                 CgState* state, double* partials, int mode,
+                                                                 const uint32_t* doneFlag) {
+    typedef typename AccOf<VT>::type AccT;
+    if (doneFlag && *(volatile const uint32_t*)doneFlag) return;
+    const int lane = threadIdx.x & 31;
+    const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
+    AccT dacc = AccT(0);
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warpsPerGrid) {
+        const int off = __ldg(&sliceOff[s]);
+        const int len = (__ldg(&sliceOff[s + 1]) - off) >> 5;
+        const int row = s * 32 + lane;
+        const VT* vp = sval + off + lane;
+        const int* cp = scol + off + lane;
+        AccT acc = AccT(0);
+        int j = 0;
+        for (; j + U <= len; j += U) {
+            VT v[U];
+            int c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                v[u] = __ldcs(vp + (j + u) * 32);
+                c[u] = __ldcs(cp + (j + u) * 32);
+            }
+            AccT xv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) xv[u] = (AccT)__ldg(&x[c[u]]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc = fma((AccT)v[u], xv[u], acc);
+        }
+        for (; j < len; ++j) acc = fma((AccT)__ldcs(vp + j * 32), (AccT)__ldg(&x[__ldcs(cp + j * 32)]), acc);
+        if (row < n) {
+            if (mode == kResidual) {
+                const AccT rv = (AccT)b[row] - acc;
+                y[row] = (VT)rv;
+                dacc = fma(rv, rv, dacc);
+            } else {
+                y[row] = (VT)acc;
+                if (mode == kCgDot) dacc = fma((AccT)x[row], acc, dacc);
+            }
+        }
+    }
+    if (mode == kPlain) return;
+    AccT v[1] = {dacc};
+    block_sum<kSellThreads, 1, AccT>(v);
+    double tot[1] = {(double)v[0]}, fin[1];
+    if (grid_sum_last<1>(tot, partials, &state->counters[0], fin)) {
+        if (threadIdx.x == 0) {
+            if (mode == kCgDot) {
+                state->pAp = fin[0];
+                state->alpha = state->rz / fin[0];
+            } else {
+                state->rrTrue = fin[0];
+            }
+        }
+    }
+}
+
+namespace {
+template <typename VT, int U>
+int sell_bps() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_sell_kernel<VT, U>, kSellThreads, 0) != cudaSuccess)
+        return 0;
+    return nb;
+}
+}  // namespace
+
+int sell_num_configs() { return 3; }
+int sell_config_unroll(int cfg) { return cfg == 0 ? 4 : (cfg == 1 ? 8 : 2); }
+
+cudaError_t sell_build(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val, int* sliceOff,
+                       int* blockSums, int64_t* total) {
+    const int nslices = (n + 31) / 32;
+    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, 152 * 64);
+    sell_slice_len_kernel<<<grid, 256, 0, st>>>(n, rowptr, sliceOff);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(sliceOff + nslices, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    e = scan_exclusive(st, sliceOff, sliceOff, nslices + 1, blockSums);
+    if (e != cudaSuccess) return e;
+    int t = 0;
+    e = cudaMemcpyAsync(&t, sliceOff + nslices, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(st);
+    *total = t;
+    return e;
+}
+
+template <typename VT>
+cudaError_t sell_fill(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val,
+                      const int* sliceOff, int* scol, VT* sval) {
+    const int nslices = (n + 31) / 32;
+    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, 152 * 64);
+    sell_fill_kernel<VT><<<grid, 256, 0, st>>>(n, rowptr, col, val, sliceOff, scol, sval);
+    return cudaGetLastError();
+}
+
+template <typename VT>
+int sell_grid(int cfg, int n, int numSms) {
+    const int u = sell_config_unroll(cfg);
+    const int bps = u == 4 ? sell_bps<VT, 4>() : (u == 8 ? sell_bps<VT, 8>() : sell_bps<VT, 2>());
+    if (bps <= 0) return 0;
+    const int nslices = (n + 31) / 32;
+    const int need = (nslices + kSellThreads / 32 - 1) / (kSellThreads / 32);
+    return std::max(1, std::min(need, bps * numSms));
+}
+
+template <typename VT>
+cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const int* sliceOff, const int* scol,
+                             const VT* sval, const VT* x, VT* y, const VT* b, CgState* state, double* partials,
+                             int mode, const uint32_t* doneFlag) {
+    if (n <= 0) return cudaSuccess;
+    const int nslices = (n + 31) / 32;
+    const int u = sell_config_unroll(cfg);
+    if (u == 4)
+        spmv_sell_kernel<VT, 4><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
+                                                              partials, mode, doneFlag);
+    else if (u == 8)
+        spmv_sell_kernel<VT, 8><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
+                                                              partials, mode, doneFlag);
+    else
+        spmv_sell_kernel<VT, 2><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
+                                                              partials, mode, doneFlag);
+    return cudaGetLastError();
+}
+
+template cudaError_t sell_fill<double>(cudaStream_t, int, const int*, const int*, const double*, const int*, int*,
+                                       double*);
+template cudaError_t sell_fill<float>(cudaStream_t, int, const int*, const int*, const double*, const int*, int*,
+                                      float*);
+template int sell_grid<double>(int, int, int);
+template int sell_grid<float>(int, int, int);
+template cudaError_t spmv_sell_launch<double>(int, int, cudaStream_t, int, const int*, const int*, const double*,
+                                              const double*, double*, const double*, CgState*, double*, int,
+                                              const uint32_t*);
+template cudaError_t spmv_sell_launch<float>(int, int, cudaStream_t, int, const int*, const int*, const float*,
+                                             const float*, float*, const float*, CgState*, double*, int,
+                                             const uint32_t*);
+
+}  // namespace xjpcg

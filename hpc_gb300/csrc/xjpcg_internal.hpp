@@ -22,6 +22,22 @@ cudaError_t spmv_launch(int cfg, int grid, cudaStream_t st, int n, const int* ro
                         const uint32_t* doneFlag);
 enum : int { kSpmvPlain = 0, kSpmvCgDot = 1, kSpmvResidual = 2 };
 
+// ---- sliced SpMV layout (spmv_kernels.cu) ----
+int sell_num_configs();
+int sell_config_unroll(int cfg);
+// sliceOff must hold nslices + 1 ints; *total = stored entries (padded).
+cudaError_t sell_build(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val, int* sliceOff,
+                       int* blockSums, int64_t* total);
+template <typename VT>
+cudaError_t sell_fill(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val,
+                      const int* sliceOff, int* scol, VT* sval);
+template <typename VT>
+int sell_grid(int cfg, int n, int numSms);
+template <typename VT>
+cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const int* sliceOff, const int* scol,
+                             const VT* sval, const VT* x, VT* y, const VT* b, CgState* state, double* partials,
+                             int mode, const uint32_t* doneFlag);
+
 // ---- CG vector kernels (cg_kernels.cu) ----
 int vec_grid(int n4, int numSms);
 cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x,

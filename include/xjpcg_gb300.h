@@ -32,7 +32,7 @@ typedef struct {
     double rrLast;         /* recursive r.r after the last iteration */
     double solveMs;        /* device time of the last solve (CUDA events) */
     uint32_t loopMode;     /* 1 = conditional-graph loop, 0 = host-driven */
-    uint32_t reserved;
+    uint32_t spmvLayout;   /* 0 = CSR staged through shared memory, 1 = sliced (SELL-32) */
 } XJPCG_GbInfo_t;
 
 /* CSR input (0- or 1-based per the mode's index nibble), same contract as
@@ -85,7 +85,8 @@ XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, in
 /* The cudaStream_t the handle launches on (for event timing by callers). */
 XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream);
 
-/* Forces the SpMV lanes-per-row (1, 2, 4, 8, 16, 32); 0 restores tuning. */
+/* Forces the CSR SpMV lanes-per-row (1, 2, 4, 8, 16, 32); -1 forces the
+ * sliced layout; 0 restores tuning. */
 XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes);
 
 #ifdef __cplusplus

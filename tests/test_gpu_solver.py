@@ -45,14 +45,17 @@ def test_diffusion27_small_csr(handle):
     _check_solve(s, r)
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32, -1])
 def test_every_spmv_shape_solves(handle, lanes):
     s = W.diffusion27(12, sigma=1.5, seed=7)
     rows, cols, vals = s.coo()
     handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 5, 1e-10)  # set the matrix
     handle.set_spmv_lanes(lanes)
     r = handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 20000, 1e-10, mode=X.MODE_KEEP_MATRIX)
-    assert handle.info().spmvLanes == lanes
+    if lanes > 0:
+        assert handle.info().spmvLanes == lanes and handle.info().spmvLayout == 0
+    else:
+        assert handle.info().spmvLayout == 1
     _check_solve(s, r)
 
 
@@ -135,15 +138,27 @@ def test_cscsym_bitexact(handle):
         _check_solve(s, res, max_iter=2000)
 
 
-def test_spmv_matches_oracle(handle):
+@pytest.mark.parametrize("lanes", [0, 1, 2, 4, 8, 16, 32, -1])
+def test_spmv_matches_oracle(handle, lanes):
     s = W.diffusion27(24, seed=5)
     rows, cols, vals = s.coo()
     handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 1, 1e-10)
+    handle.set_spmv_lanes(lanes)
     x = np.random.default_rng(1).standard_normal(s.n)
     y = handle.spmv(x)
     yref = oracle.spmv(s.rowptr, s.col, s.val, x)
     scale = oracle.spmv(s.rowptr, s.col, np.abs(s.val), np.abs(x))
     assert np.all(np.abs(y - yref) <= 1e-13 * scale)
+
+
+def test_sliced_layout_follows_value_updates(handle):
+    s = W.diffusion27(14, seed=6)
+    rows, cols, vals = s.coo()
+    handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 1, 1e-10)
+    handle.set_spmv_lanes(-1)
+    r = handle.coo_solve(s.n, None, None, vals * 3.0, s.diag * 3.0, s.b, 20000, 1e-10, mode=X.MODE_KEEP_NZ_LAYOUT)
+    assert handle.info().spmvLayout == 1
+    _check_solve(W.System(s.n, s.rowptr, s.col, s.val * 3.0, s.diag * 3.0, s.b), r)
 
 
 def test_modes_and_reuse(handle):
