@@ -321,7 +321,8 @@ def run_gb300(args):
                 "time_to_tol_s": ttt, "iters": k_iters, "iter_ms": iter_ms, "iter_gbs": iter_gbs,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
-                             "kernel": "spmv_staged_kernel (fp64 CSR SpMV)",
+                             "kernel": ("spmv_sell_kernel (sliced SELL-32 fp64 SpMV)" if info.spmvLayout == 1
+                                        else "spmv_ws_kernel (TMA-staged CSR fp64 SpMV)"),
                              "bytes_per_launch": B, "launch_ms": spmv_ms,
                              "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                              "traffic_source": traffic_src},
