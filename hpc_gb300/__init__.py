@@ -36,7 +36,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_cooSolver", "xJPCG_peekAtLastStatus", "xJPCG_getLastMessage", "xJPCG_getMetrics",
     "xJPCG_gbCsrSolver", "xJPCG_gbSolveDevice", "xJPCG_gbMixedSolve", "xJPCG_gbSpmv", "xJPCG_gbGetCsr",
     "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes",
-    "xJPCG_gbGetSpmvTuning",
+    "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc",
 ]
 
 
@@ -104,12 +104,20 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbGetStream.argtypes = [_P, C.POINTER(_P)]
     lib.xJPCG_gbSetSpmvLanes.argtypes = [_P, C.c_int]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
+    lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
         if name not in ("xJPCG_getErrorString", "xJPCG_getLastMessage"):
             fn.restype = C.c_int
     _lib = lib
     return lib
+
+
+def spmv_dot_no_alloc(n: int, d_rowptr: int, d_col: int, d_val: int, d_x: int, d_y: int, d_dot: int,
+                      stream: int = 0) -> int:
+    """xJPCG_gbSpmvDotNoAlloc: y = A x and x.y on caller-owned device memory,
+    with no device allocation (see include/xjpcg_gb300.h).  Returns the status."""
+    return load().xJPCG_gbSpmvDotNoAlloc(n, d_rowptr, d_col, d_val, d_x, d_y, d_dot, stream or None)
 
 
 def error_string(code: int) -> str:

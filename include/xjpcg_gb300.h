@@ -89,6 +89,30 @@ XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream);
  * sliced layout; 0 restores tuning. */
 XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes);
 
+/* y = A x and *d_dot = x.y for callers that cannot allocate device memory.
+ *
+ * No counterpart in the reference.  Some callers may not allocate at the
+ * point of the call: code whose framework allocator owns the device memory,
+ * code that must not synchronise the device (cudaMalloc / cudaFree can), or
+ * a thread that only owns the buffers it was handed.  They cannot create a
+ * handle, because a handle allocates.  This call takes no handle: the CSR
+ * matrix (int32 row pointers and columns, 0-based, fp64 values) and the
+ * vectors are the caller's device memory, and the kernel's only other memory
+ * (its per-CTA partial sums and a counter) is a 131328-byte static array
+ * inside this library that every GPU loading the library keeps until exit.
+ *
+ * Limit: n <= 524288 rows (one partial sum per 32-row tile, 16384 tiles);
+ * larger n returns XJPCG_STATUS_INVALID_VALUE without launching.  The call
+ * is asynchronous on `stream` (a cudaStream_t; NULL = legacy stream), with
+ * d_y and *d_dot ready when the stream reaches it.  Every call shares the
+ * static array: calls whose kernels overlap on the GPU race, calls on one
+ * stream do not.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) with that device current; make it before any stream
+ * capture.  Nothing here allocates or frees. */
+XJPCG_Status_t xJPCG_gbSpmvDotNoAlloc(uint32_t n, const int32_t* d_rowPtr, const int32_t* d_colIdx,
+                                      const double* d_values, const double* d_x, double* d_y, double* d_dot,
+                                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif
