@@ -36,7 +36,8 @@ EXPORTED_SYMBOLS = [
     "xJPCG_cooSolver", "xJPCG_peekAtLastStatus", "xJPCG_getLastMessage", "xJPCG_getMetrics",
     "xJPCG_gbCsrSolver", "xJPCG_gbSolveDevice", "xJPCG_gbMixedSolve", "xJPCG_gbSpmv", "xJPCG_gbGetCsr",
     "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes",
-    "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc",
+    "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
+    "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad",
 ]
 
 
@@ -52,7 +53,13 @@ class GbInfo(C.Structure):
                 ("spmvLanes", C.c_uint32), ("spmvGrid", C.c_uint32), ("statusBits", C.c_uint32),
                 ("outerSweeps", C.c_uint32), ("innerIters", C.c_uint32), ("bb", C.c_double),
                 ("rrLast", C.c_double), ("solveMs", C.c_double), ("loopMode", C.c_uint32),
-                ("spmvLayout", C.c_uint32)]
+                ("spmvLayout", C.c_uint32), ("batchThreads", C.c_uint32), ("batchLanes", C.c_uint32),
+                ("batchSmemRows", C.c_uint32), ("batchGrid", C.c_uint32), ("batchMs", C.c_double)]
+
+
+BATCH_RESULT_DTYPE = np.dtype([("iters", "<u4"), ("itersRun", "<u4"), ("outer", "<u4"), ("status", "<u4"),
+                               ("res", "<f8")])
+assert BATCH_RESULT_DTYPE.itemsize == 24
 
 
 RECORD_DTYPE = np.dtype([("id", "<u4"), ("iter", "<u4"), ("vecSize", "<u4"), ("maxIter", "<u4"),
@@ -105,6 +112,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbSetSpmvLanes.argtypes = [_P, C.c_int]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
+    lib.xJPCG_gbAdjointSolve.argtypes = [_P, _P, _P, _P, _P, u32, dbl, C.POINTER(u32), C.POINTER(dbl), C.c_int]
+    lib.xJPCG_gbEdgeGrad.argtypes = [_P, i64, _P, _P, _P, _P, C.c_int]
+    lib.xJPCG_gbBatchSolve.argtypes = [_P, u32, _P, _P, _P, _P, _P, _P, _P, u32, dbl, C.c_int, _P, C.c_int]
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
         if name not in ("xJPCG_getErrorString", "xJPCG_getLastMessage"):
@@ -265,6 +275,51 @@ class JPCG:
         if st != SUCCESS:
             raise XJPCGError(st, self.last_message())
         return buf[:cnt.value]
+
+    def adjoint(self, g, diag, max_iter, tol, grad_a=False):
+        """lambda = A^-1 g for the last solve's matrix; optionally dL/dA per
+        input entry.  Returns (status, lambda, gradA or None, iters, res)."""
+        n = len(g)
+        lam = np.zeros(n, np.float64)
+        ga = np.zeros(self.info().nnz, np.float64) if grad_a else None
+        it, res = C.c_uint32(0), C.c_double(0.0)
+        st = self.lib.xJPCG_gbAdjointSolve(self.h, _ptr(np.ascontiguousarray(g, np.float64)),
+                                           _ptr(np.ascontiguousarray(diag, np.float64)), _ptr(lam), _ptr(ga),
+                                           max_iter, tol, C.byref(it), C.byref(res), 0)
+        return st, lam, ga, it.value, res.value
+
+    def edge_grad(self, ei, ej, c):
+        ei = np.ascontiguousarray(ei, np.int32)
+        ej = np.ascontiguousarray(ej, np.int32)
+        c = np.ascontiguousarray(c, np.float64)
+        out = np.zeros(ei.size, np.float64)
+        st = self.lib.xJPCG_gbEdgeGrad(self.h, ei.size, _ptr(ei), _ptr(ej), _ptr(c), _ptr(out), 0)
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        return out
+
+    def batch_solve(self, systems, max_iter, tol, precision=0):
+        """Concatenates `systems` (objects with n, rowptr, col, val, diag, b),
+        solves them in one batched launch and returns (status, [x_s], results)."""
+        n = np.array([s.n for s in systems], np.int64)
+        sys_row = np.zeros(len(systems) + 1, np.int32)
+        np.cumsum(n, out=sys_row[1:])
+        nnz = np.array([s.nnz for s in systems], np.int64)
+        offs = np.zeros(len(systems) + 1, np.int64)
+        np.cumsum(nnz, out=offs[1:])
+        rowptr = np.concatenate([systems[0].rowptr[:1].astype(np.int64) * 0] +
+                                [s.rowptr[1:].astype(np.int64) + offs[i] for i, s in enumerate(systems)])
+        rowptr = rowptr.astype(np.int32)
+        col = np.concatenate([s.col for s in systems]).astype(np.int32)
+        val = np.concatenate([s.val for s in systems])
+        diag = np.concatenate([s.diag for s in systems])
+        b = np.concatenate([s.b for s in systems])
+        x = np.zeros(int(sys_row[-1]), np.float64)
+        res = np.zeros(len(systems), BATCH_RESULT_DTYPE)
+        st = self.lib.xJPCG_gbBatchSolve(self.h, len(systems), _ptr(sys_row), _ptr(rowptr), _ptr(col), _ptr(val),
+                                         _ptr(diag), _ptr(b), _ptr(x), max_iter, tol, precision, _ptr(res), 0)
+        xs = [x[sys_row[i]:sys_row[i + 1]] for i in range(len(systems))]
+        return st, xs, res
 
     def spmv_tuning(self):
         """[(lanes, consumers, chunk, stages, ms)] of the last SpMV tuning."""

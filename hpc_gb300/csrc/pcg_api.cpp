@@ -43,6 +43,7 @@ void finishSolve(PcgHandle* p, const xjpcg::Results& r, double tol, double* res,
     if (iter32) *iter32 = r.reportedIters;
     if (iter64) *iter64 = r.reportedIters;
     p->markCalled();
+    p->markSolved();
     p->metrics()->m_solver = elapsed(last);
     if (r.status & xjpcg::kStatusBreakdown)
         throw xjpcg::ExecFailed("breakdown (non-finite alpha, beta or r.r) after " + std::to_string(r.reportedIters) +
@@ -291,6 +292,7 @@ XJPCG_Status_t xJPCG_gbMixedSolve(XJPCG_Handle_t* handle, const double* b, const
     p->metrics()->m_vecProc = elapsed(last);
     xjpcg::Results r = p->runMixed(maxIter, tol);
     if (x) p->copyX64(x, p->matrixN(), onDevice != 0);
+    p->markSolved();
     *res = std::sqrt(r.rrLast / r.bb);
     if (iter) *iter = r.reportedIters;
     p->metrics()->m_solver = elapsed(last);
@@ -299,6 +301,48 @@ XJPCG_Status_t xJPCG_gbMixedSolve(XJPCG_Handle_t* handle, const double* b, const
         throw xjpcg::ExecFailed("exit with divergent solution after " + std::to_string(r.reportedIters) +
                                 " inner iterations.");
     XJ_GUARD_END("Solver returns successfully")
+}
+
+XJPCG_Status_t xJPCG_gbAdjointSolve(XJPCG_Handle_t* handle, const double* g, const double* diagA, double* lambda,
+                                    double* gradA, uint32_t maxIter, double tol, uint32_t* iter, double* res,
+                                    int onDevice) {
+    XJ_GUARD_BEGIN
+    auto last = std::chrono::high_resolution_clock::now();
+    if (g == nullptr || diagA == nullptr) throw xjpcg::InvalidValue("Vector is nullptr.");
+    xjpcg::Results r = p->adjoint(g, diagA, lambda, gradA, maxIter, tol, onDevice != 0);
+    *res = std::sqrt(r.rrLast / r.bb);
+    if (iter) *iter = r.reportedIters;
+    p->metrics()->m_solver = elapsed(last);
+    if (r.status & xjpcg::kStatusBreakdown) throw xjpcg::ExecFailed("breakdown in the adjoint solve.");
+    if (*res > tol)
+        throw xjpcg::ExecFailed("adjoint exit with divergent solution after " + std::to_string(r.reportedIters) +
+                                " iterations.");
+    XJ_GUARD_END("Adjoint solver returns successfully")
+}
+
+XJPCG_Status_t xJPCG_gbEdgeGrad(XJPCG_Handle_t* handle, int64_t numEdges, const int32_t* edgeI, const int32_t* edgeJ,
+                                const double* conductance, double* gradTheta, int onDevice) {
+    XJ_GUARD_BEGIN
+    if (edgeI == nullptr || edgeJ == nullptr || conductance == nullptr || gradTheta == nullptr)
+        throw xjpcg::InvalidValue("edge array is nullptr.");
+    p->edgeGrad(numEdges, edgeI, edgeJ, conductance, gradTheta, onDevice != 0);
+    XJ_GUARD_END("Edge gradient returns successfully")
+}
+
+XJPCG_Status_t xJPCG_gbBatchSolve(XJPCG_Handle_t* handle, uint32_t numSystems, const int32_t* sysRowStart,
+                                  const int32_t* rowPtr, const int32_t* colIdx, const double* values,
+                                  const double* diagA, const double* b, double* x, uint32_t maxIter, double tol,
+                                  int precision, XJPCG_GbBatchResult_t* results, int onDevice) {
+    XJ_GUARD_BEGIN
+    if (sysRowStart == nullptr || rowPtr == nullptr || colIdx == nullptr || values == nullptr)
+        throw xjpcg::InvalidValue("Matrix is nullptr.");
+    if (diagA == nullptr || b == nullptr) throw xjpcg::InvalidValue("Vector is nullptr.");
+    static_assert(sizeof(XJPCG_GbBatchResult_t) == sizeof(xjpcg::BatchResult), "result layout");
+    const uint32_t failed = p->batchSolve(numSystems, sysRowStart, rowPtr, colIdx, values, diagA, b, x, maxIter, tol,
+                                          precision, reinterpret_cast<xjpcg::BatchResult*>(results), onDevice != 0);
+    if (failed) throw xjpcg::ExecFailed(std::to_string(failed) + " of " + std::to_string(numSystems) +
+                                        " systems did not reach the tolerance.");
+    XJ_GUARD_END("Batched solver returns successfully")
 }
 
 XJPCG_Status_t xJPCG_gbSpmv(XJPCG_Handle_t* handle, const double* x, double* y, int onDevice) {

@@ -709,6 +709,221 @@ void PcgHandle::spmv(const double* x, double* y, bool onDevice) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint
+// ---------------------------------------------------------------------------
+Results PcgHandle::adjoint(const double* g, const double* diag, double* lambda, double* gradA, uint32_t maxIter,
+                           double tol, bool onDevice) {
+    if (!m_haveMatrix || !m_haveX) throw InvalidValue("the adjoint needs a completed solve on this handle.");
+    const size_t vb = sizeof(double) * ((size_t)m_n4 + 4);
+    alloc(m_xKeep, vb, "adjoint x");
+    alloc(m_lambda, vb, "adjoint lambda");
+    check(cudaMemcpyAsync(m_xKeep.p, m_x.p, vb, cudaMemcpyDeviceToDevice, m_stream), "keep x");
+    setVec(m_n, g, diag, onDevice);
+    Results r = run(maxIter, tol);
+    check(cudaMemcpyAsync(m_lambda.p, m_x.p, vb, cudaMemcpyDeviceToDevice, m_stream), "lambda");
+    check(cudaMemcpyAsync(m_x.p, m_xKeep.p, vb, cudaMemcpyDeviceToDevice, m_stream), "restore x");
+    m_haveLambda = true;
+    const cudaMemcpyKind out = onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (lambda) check(cudaMemcpyAsync(lambda, m_lambda.p, sizeof(double) * m_n, out, m_stream), "copy lambda");
+    if (gradA) {
+        // dL/dA per input entry: COO / CSR inputs index gradA like their data
+        // array (perm maps CSR slots back); symmetric CSC input indexes it by
+        // the expanded full matrix (2 nnz - n entries, emission order).
+        alloc(m_grad, sizeof(double) * (m_nnz + 4), "dA");
+        check(grad_nnz_launch(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_perm.as<uint32_t>(),
+                              m_xKeep.as<double>(), m_lambda.as<double>(), m_grad.as<double>()),
+              "dA kernel");
+        check(cudaMemcpyAsync(gradA, m_grad.p, sizeof(double) * m_nnz, out, m_stream), "copy dA");
+    }
+    check(cudaStreamSynchronize(m_stream), "sync");
+    return r;
+}
+
+void PcgHandle::edgeGrad(int64_t m, const int32_t* ei, const int32_t* ej, const double* c, double* grad,
+                         bool onDevice) {
+    if (!m_haveLambda) throw InvalidValue("the edge gradient needs a completed adjoint solve.");
+    if (m <= 0) throw InvalidValue("number of edges must be positive.");
+    const int* dI = ei;
+    const int* dJ = ej;
+    const double* dC = c;
+    double* dG = grad;
+    if (!onDevice) {
+        alloc(m_edgeI, sizeof(int) * m, "edges");
+        alloc(m_edgeJ, sizeof(int) * m, "edges");
+        alloc(m_edgeC, sizeof(double) * m, "edges");
+        alloc(m_edgeG, sizeof(double) * m, "edge gradient");
+        check(cudaMemcpyAsync(m_edgeI.p, ei, sizeof(int) * m, cudaMemcpyHostToDevice, m_stream), "H2D");
+        check(cudaMemcpyAsync(m_edgeJ.p, ej, sizeof(int) * m, cudaMemcpyHostToDevice, m_stream), "H2D");
+        check(cudaMemcpyAsync(m_edgeC.p, c, sizeof(double) * m, cudaMemcpyHostToDevice, m_stream), "H2D");
+        dI = m_edgeI.as<int>();
+        dJ = m_edgeJ.as<int>();
+        dC = m_edgeC.as<double>();
+        dG = m_edgeG.as<double>();
+    }
+    int bad = 0;
+    check(edge_grad_launch(m_stream, m, (int)m_n, dI, dJ, dC, m_x.as<double>(), m_lambda.as<double>(), dG,
+                           m_flags.as<int>(), &bad),
+          "edge gradient");
+    if (bad) throw InvalidValue("an edge endpoint lies outside [0, n).");
+    if (!onDevice) check(cudaMemcpyAsync(grad, dG, sizeof(double) * m, cudaMemcpyDeviceToHost, m_stream), "D2H");
+    check(cudaStreamSynchronize(m_stream), "sync");
+}
+
+// ---------------------------------------------------------------------------
+// Batched solves
+// ---------------------------------------------------------------------------
+namespace {
+__attribute__((unused)) uint64_t mixKey(uint64_t h, uint64_t v) { return (h ^ v) * 0x100000001b3ull; }
+}  // namespace
+
+uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32_t* rowPtr, const int32_t* colIdx,
+                               const double* values, const double* diag, const double* b, double* x,
+                               uint32_t maxIter, double tol, int precision, BatchResult* results, bool onDevice) {
+    if (nsys == 0) throw InvalidValue("number of systems is zero.");
+    if (precision != 0 && precision != 1) throw InvalidValue("precision must be 0 (fp64) or 1 (mixed).");
+    const bool mixed = precision == 1;
+    // System and row offsets are small: validate them on the host.
+    std::vector<int32_t> hSys(nsys + 1);
+    check(cudaMemcpy(hSys.data(), sysRow, sizeof(int32_t) * (nsys + 1), onDevice ? cudaMemcpyDeviceToHost
+                                                                                  : cudaMemcpyHostToHost),
+          "system offsets");
+    if (hSys[0] != 0) throw InvalidValue("system row offsets must start at 0.");
+    int maxN = 0;
+    for (uint32_t s = 0; s < nsys; ++s) {
+        const int ns = hSys[s + 1] - hSys[s];
+        if (ns <= 0) throw InvalidValue("every system needs at least one row.");
+        maxN = std::max(maxN, ns);
+    }
+    const int total = hSys[nsys];
+    std::vector<int32_t> hRp((size_t)total + 1);
+    check(cudaMemcpy(hRp.data(), rowPtr, sizeof(int32_t) * ((size_t)total + 1),
+                     onDevice ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost),
+          "row pointers");
+    if (hRp[0] != 0) throw InvalidValue("row pointers must start at 0.");
+    for (int i = 0; i < total; ++i)
+        if (hRp[i + 1] < hRp[i]) throw InvalidValue("row pointers are not monotone.");
+    const int64_t nnz = hRp[total];
+    // Queue order: largest systems first so the long solves start early.
+    std::vector<int32_t> order(nsys);
+    for (uint32_t s = 0; s < nsys; ++s) order[s] = (int32_t)s;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t c) {
+        return (hRp[hSys[a + 1]] - hRp[hSys[a]]) > (hRp[hSys[c + 1]] - hRp[hSys[c]]);
+    });
+    const size_t vb = sizeof(double) * ((size_t)total + 4), fb = sizeof(float) * ((size_t)total + 4);
+    alloc(m_bSysRow, sizeof(int32_t) * (nsys + 1), "batch offsets");
+    alloc(m_bOrder, sizeof(int32_t) * nsys, "batch order");
+    alloc(m_bRowptr, sizeof(int32_t) * ((size_t)total + 1), "batch row pointers");
+    alloc(m_bCol, sizeof(int32_t) * ((size_t)nnz + 4), "batch columns");
+    alloc(m_bVal, sizeof(double) * ((size_t)nnz + 4), "batch values");
+    for (DevBuf* v : {&m_bB, &m_bDiag, &m_bX, &m_bR, &m_bAp, &m_bJ, &m_bP}) alloc(*v, vb, "batch vector");
+    if (mixed) {
+        alloc(m_bVal32, sizeof(float) * ((size_t)nnz + 4), "batch fp32 values");
+        for (DevBuf* v : {&m_bR32, &m_bD32, &m_bAp32, &m_bJ32, &m_bP32}) alloc(*v, fb, "batch vector");
+    }
+    alloc(m_bRes, sizeof(BatchResult) * nsys, "batch results");
+    alloc(m_bQueue, 16, "batch queue");
+    const cudaMemcpyKind k = onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    check(cudaMemcpyAsync(m_bSysRow.p, hSys.data(), sizeof(int32_t) * (nsys + 1), cudaMemcpyHostToDevice, m_stream),
+          "H2D");
+    check(cudaMemcpyAsync(m_bOrder.p, order.data(), sizeof(int32_t) * nsys, cudaMemcpyHostToDevice, m_stream), "H2D");
+    check(cudaMemcpyAsync(m_bRowptr.p, hRp.data(), sizeof(int32_t) * ((size_t)total + 1), cudaMemcpyHostToDevice,
+                          m_stream),
+          "H2D");
+    check(cudaMemcpyAsync(m_bCol.p, colIdx, sizeof(int32_t) * nnz, k, m_stream), "copy columns");
+    check(cudaMemcpyAsync(m_bVal.p, values, sizeof(double) * nnz, k, m_stream), "copy values");
+    check(cudaMemcpyAsync(m_bB.p, b, sizeof(double) * total, k, m_stream), "copy b");
+    check(cudaMemcpyAsync(m_bDiag.p, diag, sizeof(double) * total, k, m_stream), "copy diag");
+    check(batch_validate_columns(m_stream, (int)nsys, m_bSysRow.as<int>(), m_bRowptr.as<int>(), m_bCol.as<int>(),
+                                 m_flags.as<int>()),
+          "column check");
+    int bad = 0;
+    check(cudaMemcpyAsync(&bad, m_flags.p, sizeof(int), cudaMemcpyDeviceToHost, m_stream), "D2H");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    if (bad) throw InvalidValue("a column index lies outside its system.");
+    if (mixed) check(convert_f64_to_f32(m_stream, nnz, m_bVal.as<double>(), m_bVal32.as<float>()), "fp32 values");
+
+    BatchLaunch L;
+    L.nsys = (int)nsys;
+    L.sysRow = m_bSysRow.as<int>();
+    L.order = m_bOrder.as<int>();
+    L.rowptr = m_bRowptr.as<int>();
+    L.col = m_bCol.as<int>();
+    L.val = m_bVal.as<double>();
+    L.val32 = mixed ? m_bVal32.as<float>() : nullptr;
+    L.b = m_bB.as<double>();
+    L.diag = m_bDiag.as<double>();
+    L.x = m_bX.as<double>();
+    L.r = m_bR.as<double>();
+    L.Ap = m_bAp.as<double>();
+    L.J = m_bJ.as<double>();
+    L.r32 = mixed ? m_bR32.as<float>() : nullptr;
+    L.d32 = mixed ? m_bD32.as<float>() : nullptr;
+    L.Ap32 = mixed ? m_bAp32.as<float>() : nullptr;
+    L.J32 = mixed ? m_bJ32.as<float>() : nullptr;
+    L.pGlobal = m_bP.as<double>();
+    L.p32Global = mixed ? m_bP32.as<float>() : nullptr;
+    L.res = m_bRes.as<BatchResult>();
+    L.queue = m_bQueue.as<uint32_t>();
+    L.maxIterP1 = maxIter + 1u;
+    L.tol = tol;
+    L.innerTol = envDouble("XJPCG_INNER_TOL", 1e-5);
+
+    // Shape candidates: CTA size x lanes per row x rows of p kept in shared
+    // memory (the largest system, or a third of it for more CTAs per SM).
+    const size_t esz = mixed ? sizeof(float) : sizeof(double);
+    const int smemCap = (int)(200 * 1024 / esz);
+    std::vector<int> smemRows = {std::min(maxN, smemCap), std::min(maxN, 4096)};
+    if (smemRows[1] == smemRows[0]) smemRows.pop_back();
+    const uint64_t key = mixKey(mixKey(mixKey(nsys, (uint64_t)total), (uint64_t)nnz), (uint64_t)precision + 7);
+    const int forced = envInt("XJPCG_BATCH_CFG", -1);
+    auto runOnce = [&](int cfg, int rows, float* ms) {
+        check(cudaMemsetAsync(m_bQueue.p, 0, 16, m_stream), "memset queue");
+        check(cudaEventRecord(m_ev0, m_stream), "event");
+        int grid = 0;
+        check(batch_launch(cfg, mixed, m_numSms, rows, m_stream, L, &grid), "batched kernel");
+        check(cudaEventRecord(m_ev1, m_stream), "event");
+        check(cudaEventSynchronize(m_ev1), "event");
+        check(cudaEventElapsedTime(ms, m_ev0, m_ev1), "event");
+        m_batchGrid = grid;
+    };
+    const int ncfg = batch_num_configs();
+    if (forced >= 0 && forced < ncfg * (int)smemRows.size()) {
+        m_batchCfg = forced % ncfg;
+        m_batchSmemRows = smemRows[forced / ncfg];
+    } else if (m_batchKey != key || m_batchCfg < 0) {
+        m_batchTuneMs.assign((size_t)ncfg * smemRows.size(), -1.f);
+        float best = 1e30f;
+        for (size_t si = 0; si < smemRows.size(); ++si)
+            for (int c = 0; c < ncfg; ++c) {
+                float ms = 0;
+                runOnce(c, smemRows[si], &ms);
+                m_batchTuneMs[si * ncfg + c] = ms;
+                if (ms < best) {
+                    best = ms;
+                    m_batchCfg = c;
+                    m_batchSmemRows = smemRows[si];
+                }
+            }
+        m_batchKey = key;
+    }
+    runOnce(m_batchCfg, m_batchSmemRows, &m_batchMs);
+    std::vector<BatchResult> hr(nsys);
+    check(cudaMemcpyAsync(results ? (void*)results : (void*)hr.data(), m_bRes.p, sizeof(BatchResult) * nsys,
+                          cudaMemcpyDeviceToHost, m_stream),
+          "D2H results");
+    if (x)
+        check(cudaMemcpyAsync(x, m_bX.p, sizeof(double) * total, onDevice ? cudaMemcpyDeviceToDevice
+                                                                          : cudaMemcpyDeviceToHost, m_stream),
+              "copy x");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    const BatchResult* rr = results ? results : hr.data();
+    uint32_t failed = 0;
+    for (uint32_t s = 0; s < nsys; ++s)
+        if (rr[s].status != 0 || !(rr[s].res <= tol)) ++failed;
+    return failed;
+}
+
 void PcgHandle::getCsr(int32_t* rowPtr, int32_t* colIdx, double* values, uint32_t* perm) {
     if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
     if (rowPtr)
@@ -763,6 +978,15 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->rrLast = m_lastState.rr;
     info->solveMs = m_lastMs;
     info->loopMode = m_useGraph ? 1u : 0u;
+    if (m_batchCfg >= 0) {
+        int t = 0, l = 0;
+        batch_config_shape(m_batchCfg, &t, &l);
+        info->batchThreads = (uint32_t)t;
+        info->batchLanes = (uint32_t)l;
+    }
+    info->batchSmemRows = (uint32_t)m_batchSmemRows;
+    info->batchGrid = (uint32_t)m_batchGrid;
+    info->batchMs = m_batchMs;
 }
 
 }  // namespace xjpcg

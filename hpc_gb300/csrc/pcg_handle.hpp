@@ -84,6 +84,16 @@ class PcgHandle {
     void copyX64(double* x, uint32_t n, bool toDevice);
 
     void spmv(const double* x, double* y, bool onDevice);
+    // Adjoint of the last solve: lambda = A^-1 g; optional dL/dA per input entry.
+    Results adjoint(const double* g, const double* diag, double* lambda, double* gradA, uint32_t maxIter, double tol,
+                    bool onDevice);
+    void edgeGrad(int64_t m, const int32_t* ei, const int32_t* ej, const double* c, double* grad, bool onDevice);
+    void markSolved() { m_haveX = true; }
+    // Batched solve: concatenated systems (see batched_kernels.cu).  Returns the
+    // number of systems that did not converge.
+    uint32_t batchSolve(uint32_t nsys, const int32_t* sysRow, const int32_t* rowPtr, const int32_t* colIdx,
+                        const double* values, const double* diag, const double* b, double* x, uint32_t maxIter,
+                        double tol, int precision, BatchResult* results, bool onDevice);
     void getCsr(int32_t* rowPtr, int32_t* colIdx, double* values, uint32_t* perm);
     uint64_t getRecords(void* buf, uint64_t cap);
     void fillInfo(XJPCG_GbInfo_t* info) const;
@@ -167,6 +177,18 @@ class PcgHandle {
     DevBuf m_scratchY;
     // mixed precision
     DevBuf m_state32, m_r32, m_p32, m_d32, m_Ap32, m_J32;
+
+    // adjoint
+    DevBuf m_xKeep, m_lambda, m_grad, m_edgeI, m_edgeJ, m_edgeC, m_edgeG;
+    bool m_haveX = false, m_haveLambda = false;
+
+    // batched solves
+    DevBuf m_bSysRow, m_bOrder, m_bRowptr, m_bCol, m_bVal, m_bVal32, m_bB, m_bDiag, m_bX, m_bR, m_bAp, m_bJ;
+    DevBuf m_bR32, m_bD32, m_bAp32, m_bJ32, m_bP, m_bP32, m_bRes, m_bQueue;
+    int m_batchCfg = -1, m_batchSmemRows = 0, m_batchGrid = 0;
+    uint64_t m_batchKey = 0;
+    float m_batchMs = 0.f;
+    std::vector<float> m_batchTuneMs;
 
     // graph
     cudaGraphExec_t m_exec = nullptr;

@@ -61,6 +61,53 @@ cudaError_t cg32_pupdate_launch(int grid, cudaStream_t s, int n4, float* p, cons
 cudaError_t ir_update_launch(int grid, cudaStream_t s, int n4, double* x, const float* d, CgState* st,
                              const CgState* in);
 
+// ---- batched solves (batched_kernels.cu) ----
+struct BatchResult {      // layout of XJPCG_GbBatchResult_t
+    uint32_t iters;       // reported iterations (min(K, maxIter)); mixed: inner iterations
+    uint32_t itersRun;    // iterations executed (K)
+    uint32_t outer;       // mixed: refinement sweeps
+    uint32_t status;      // 0 ok, 1 breakdown (non-finite alpha / beta / r.r)
+    double res;           // fp64: sqrt(r.r / b.b) of the recursive residual; mixed: true residual
+};
+struct BatchLaunch {
+    int nsys;
+    const int* sysRow;
+    const int* order;
+    const int* rowptr;
+    const int* col;
+    const double* val;
+    const float* val32;
+    const double* b;
+    const double* diag;
+    double* x;
+    double* r;
+    double* Ap;
+    double* J;
+    float* r32;
+    float* d32;
+    float* Ap32;
+    float* J32;
+    double* pGlobal;
+    float* p32Global;
+    BatchResult* res;
+    uint32_t* queue;
+    uint32_t maxIterP1;
+    double tol;
+    double innerTol;
+};
+int batch_num_configs();
+cudaError_t batch_validate_columns(cudaStream_t st, int nsys, const int* sysRow, const int* rowptr, const int* col,
+                                   int* flag);
+void batch_config_shape(int cfg, int* threads, int* lanes);
+cudaError_t batch_launch(int cfg, bool mixed, int numSms, int smemRows, cudaStream_t st, const BatchLaunch& L,
+                         int* gridOut);
+
+// ---- adjoint (adjoint_kernels.cu) ----
+cudaError_t grad_nnz_launch(cudaStream_t st, int n, const int* rowptr, const int* col, const uint32_t* perm,
+                            const double* x, const double* lambda, double* grad);
+cudaError_t edge_grad_launch(cudaStream_t st, int64_t m, int n, const int* ei, const int* ej, const double* c,
+                             const double* x, const double* lambda, double* grad, int* flag, int* hostBad);
+
 // ---- conversion (convert_kernels.cu) ----
 // All return cudaSuccess or the first CUDA error; data errors are reported
 // through *errFlag (device int) as kStatusIndexError / kStatusCountError.

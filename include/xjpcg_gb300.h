@@ -33,7 +33,21 @@ typedef struct {
     double solveMs;        /* device time of the last solve (CUDA events) */
     uint32_t loopMode;     /* 1 = conditional-graph loop, 0 = host-driven */
     uint32_t spmvLayout;   /* 0 = CSR staged through shared memory, 1 = sliced (SELL-32) */
+    uint32_t batchThreads; /* batched solves: CTA size chosen by the tuner */
+    uint32_t batchLanes;   /* batched solves: lanes per row */
+    uint32_t batchSmemRows;/* batched solves: rows of p held in shared memory */
+    uint32_t batchGrid;    /* batched solves: CTAs of the persistent launch */
+    double batchMs;        /* batched solves: device time of the last batch (CUDA events) */
 } XJPCG_GbInfo_t;
+
+/* Per-system outcome of a batched solve. */
+typedef struct {
+    uint32_t iters;    /* fp64: min(K, maxIter) as xJPCG reports it; mixed: inner iterations */
+    uint32_t itersRun; /* iterations executed (fp64: K) */
+    uint32_t outer;    /* mixed: refinement sweeps */
+    uint32_t status;   /* 0 = ran to its stop rule, 1 = breakdown (non-finite alpha, beta or r.r) */
+    double res;        /* fp64: sqrt(r.r / b.b) of the recursive residual; mixed: true relative residual */
+} XJPCG_GbBatchResult_t;
 
 /* CSR input (0- or 1-based per the mode's index nibble), same contract as
  * xJPCG_cooSolver otherwise.  The row pointer and column arrays are int32.
@@ -57,6 +71,43 @@ XJPCG_Status_t xJPCG_gbSolveDevice(XJPCG_Handle_t* handle, const double* d_b, co
  * residual.  onDevice != 0: b, diagA and x are device pointers. */
 XJPCG_Status_t xJPCG_gbMixedSolve(XJPCG_Handle_t* handle, const double* b, const double* diagA, double* x,
                                   uint32_t maxIter, double tol, uint32_t* iter, double* res, int onDevice);
+
+/* Adjoint of the handle's last solve x = A^-1 b (no counterpart in the
+ * reference).  With g = dL/dx, solves lambda = A^-1 g (A is SPD) with the
+ * same fp64 JPCG and stop rule, then, when gradA is not NULL, writes
+ * dL/dA = -lambda_i x_j for every stored entry: for COO / CSR input gradA is
+ * indexed like the input data array (duplicates each get the full value); for
+ * symmetric-CSC input it is indexed by the expanded full matrix in the
+ * reference's emission order (2 nnz - n entries).  dL/db = lambda.  Only the
+ * converged x and lambda are kept.  onDevice != 0: g, diagA, lambda and
+ * gradA are device pointers. */
+XJPCG_Status_t xJPCG_gbAdjointSolve(XJPCG_Handle_t* handle, const double* g, const double* diagA, double* lambda,
+                                    double* gradA, uint32_t maxIter, double tol, uint32_t* iter, double* res,
+                                    int onDevice);
+
+/* Edge gradient of a diffusion parametrisation (no counterpart in the
+ * reference): for A = sum_e c_e (e_i - e_j)(e_i - e_j)^T + G with
+ * c_e = exp(theta_e), writes gradTheta[e] = -c_e (lambda_i - lambda_j)
+ * (x_i - x_j) = dL/dtheta_e, from the last solve's x and the last adjoint's
+ * lambda.  onDevice != 0: the edge arrays are device pointers. */
+XJPCG_Status_t xJPCG_gbEdgeGrad(XJPCG_Handle_t* handle, int64_t numEdges, const int32_t* edgeI, const int32_t* edgeJ,
+                                const double* conductance, double* gradTheta, int onDevice);
+
+/* Solves numSystems independent SPD systems in one persistent launch (no
+ * counterpart in the reference; its control loop carries a CG_numTasks hook,
+ * pcg/hw/include/control.hpp:43-92, built with one task).  The systems are
+ * concatenated: system s owns rows sysRowStart[s] .. sysRowStart[s+1]-1 of the
+ * concatenated vectors; rowPtr holds global entry offsets (rowPtr[0] = 0) and
+ * colIdx holds 0-based column indices local to the system.  Every system uses
+ * the xJPCG stop rule (fp64, precision 0) or FP64 refinement around an FP32
+ * inner CG (precision 1), x0 = 0, with its own convergence test; results[s]
+ * reports it.  Returns SUCCESS when every system met tol, else
+ * EXECUTION_FAILED (x and results are written either way).  onDevice != 0:
+ * all arrays except results are device pointers. */
+XJPCG_Status_t xJPCG_gbBatchSolve(XJPCG_Handle_t* handle, uint32_t numSystems, const int32_t* sysRowStart,
+                                  const int32_t* rowPtr, const int32_t* colIdx, const double* values,
+                                  const double* diagA, const double* b, double* x, uint32_t maxIter, double tol,
+                                  int precision, XJPCG_GbBatchResult_t* results, int onDevice);
 
 /* y = A x with the stored matrix.  onDevice != 0: x and y are device
  * pointers (no host copies). */

@@ -1,0 +1,62 @@
+"""Batched JPCG (one persistent launch, per-system convergence) against the
+oracle, system by system: fp64 with the xJPCG bar (iterations within 1 %,
+x within 1e-8, true residual 1e-10) and the FP32-inner / FP64-refinement
+form against a tight FP64 oracle solve."""
+import numpy as np
+import pytest
+
+import hpc_gb300 as X
+import oracle
+from hpc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def batch():
+    return W.batched_stencils(count=48, lo=200, hi=4000, seed=3)
+
+
+def test_batched_fp64_matches_oracle(handle, batch):
+    st, xs, res = handle.batch_solve(batch, 20000, 1e-10, precision=0)
+    assert st == X.SUCCESS, handle.last_message()
+    for s, x, r in zip(batch, xs, res):
+        ref = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
+        assert r["status"] == 0
+        assert abs(int(r["iters"]) - ref["iters"]) <= max(1, int(0.01 * ref["iters"])), (r["iters"], ref["iters"])
+        err = np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"])
+        assert err <= 1e-8, err
+        assert oracle.true_relres(s.rowptr, s.col, s.val, s.b, x) <= 1.5e-10
+        assert r["res"] <= 1e-10
+
+
+def test_batched_mixed_reaches_fp64_accuracy(handle, batch):
+    st, xs, res = handle.batch_solve(batch, 20000, 1e-10, precision=1)
+    assert st == X.SUCCESS, handle.last_message()
+    for s, x, r in zip(batch, xs, res):
+        rel = oracle.true_relres(s.rowptr, s.col, s.val, s.b, x)
+        assert rel <= 1.5e-10, rel
+        assert r["outer"] >= 1 and r["status"] == 0
+        tight = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 200000, 1e-14)
+        ref64 = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
+        err = np.linalg.norm(x - tight["x"]) / np.linalg.norm(tight["x"])
+        err64 = np.linalg.norm(ref64["x"] - tight["x"]) / np.linalg.norm(tight["x"])
+        assert err <= max(10 * err64, 1e-9), (err, err64)
+
+
+def test_batched_maxiter_and_mask(handle, batch):
+    # a cap of 5 iterations: every system stops on its own at the cap and
+    # reports it the way xJPCG does (iters = maxIter, K = maxIter + 1)
+    st, xs, res = handle.batch_solve(batch[:8], 5, 1e-10, precision=0)
+    assert st == X.EXECUTION_FAILED
+    for s, x, r in zip(batch[:8], xs, res):
+        ref = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 5, 1e-10)
+        assert int(r["iters"]) == ref["iters"] == 5 and int(r["itersRun"]) == ref["k"] == 6
+        assert abs(r["res"] - ref["res"]) <= 1e-9 * ref["res"]
+
+
+def test_batched_rejects_bad_columns(handle, batch):
+    bad = [W.System(s.n, s.rowptr, s.col.copy(), s.val, s.diag, s.b) for s in batch[:2]]
+    bad[1].col[3] = bad[1].n  # outside its own system
+    st, _, _ = handle.batch_solve(bad, 100, 1e-10)
+    assert st == X.INVALID_VALUE
