@@ -10,8 +10,8 @@
 //     ir_inner_init              r32 = s r, p32 = J32 r32, d32 = 0, r.z
 //     WHILE inner:
 //       SpMV fp32, kCgDot        Ap = A p, p.Ap, alpha          (FP32 data)
-//       cg32_update              d += alpha p, r -= alpha Ap, r.r, r.z, beta
-//       cg32_pupdate             p = J r + beta p
+//       cg32_update              r -= alpha Ap, r.r, r.z, beta
+//       cg32_pupdate             d += alpha p, p = J r + beta p
 //     ir_update                  x += d / s                     (FP64)
 //
 // FP64 is kept for the true residual, the outer x update and the alpha/beta
@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(kMxThreads) ir_inner_init_kernel(int n4, const
         in->rz = fin[1];
         in->tols = fin[0] * innerTol * innerTol;
         in->k = 0;
+        in->xTag = 0;
         const uint32_t used = st->innerK;
         const uint32_t budget = st->maxIterP1 - 1u;  // user maxIter
         in->maxIterP1 = budget > used ? budget - used : 1u;
@@ -112,8 +113,7 @@ __global__ void __launch_bounds__(kMxThreads) ir_inner_init_kernel(int n4, const
     }
 }
 
-__global__ void __launch_bounds__(kMxThreads) cg32_update_kernel(int n4, float* __restrict__ d, float* __restrict__ r,
-                                                                 const float* __restrict__ p,
+__global__ void __launch_bounds__(kMxThreads) cg32_update_kernel(int n4, float* __restrict__ r,
                                                                  const float* __restrict__ Ap,
                                                                  const float* __restrict__ J, CgState* in,
                                                                  double* partials, uint64_t innerHandle, int useCond) {
@@ -127,18 +127,12 @@ __global__ void __launch_bounds__(kMxThreads) cg32_update_kernel(int n4, float* 
     const float alpha = (float)alphaD;
     float rr = 0.f, rz = 0.f;
     const int n4q = n4 >> 2;
-    float4* d4 = reinterpret_cast<float4*>(d);
     float4* r4 = reinterpret_cast<float4*>(r);
-    const float4* p4 = reinterpret_cast<const float4*>(p);
     const float4* a4 = reinterpret_cast<const float4*>(Ap);
     const float4* j4 = reinterpret_cast<const float4*>(J);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4q; i += gridDim.x * blockDim.x) {
-        float4 dv = d4[i], rv = r4[i];
-        const float4 pv = p4[i], av = __ldcs(&a4[i]), jv = j4[i];
-        dv.x = fmaf(alpha, pv.x, dv.x);
-        dv.y = fmaf(alpha, pv.y, dv.y);
-        dv.z = fmaf(alpha, pv.z, dv.z);
-        dv.w = fmaf(alpha, pv.w, dv.w);
+        float4 rv = r4[i];
+        const float4 av = __ldcs(&a4[i]), jv = j4[i];
         rv.x = fmaf(-alpha, av.x, rv.x);
         rv.y = fmaf(-alpha, av.y, rv.y);
         rv.z = fmaf(-alpha, av.z, rv.z);
@@ -151,7 +145,6 @@ __global__ void __launch_bounds__(kMxThreads) cg32_update_kernel(int n4, float* 
         rz = fmaf(rv.y, rv.y * jv.y, rz);
         rz = fmaf(rv.z, rv.z * jv.z, rz);
         rz = fmaf(rv.w, rv.w * jv.w, rz);
-        d4[i] = dv;
         r4[i] = rv;
     }
     float v[2] = {rr, rz};
@@ -172,23 +165,48 @@ __global__ void __launch_bounds__(kMxThreads) cg32_update_kernel(int n4, float* 
     }
 }
 
-__global__ void __launch_bounds__(kMxThreads) cg32_pupdate_kernel(int n4, float* __restrict__ p,
+// d += alpha p (moved here from the update kernel, where p is not otherwise
+// read), then p = J r + beta p unless the inner loop just stopped; the
+// iteration tag keeps the d update from being applied twice.
+__global__ void __launch_bounds__(kMxThreads) cg32_pupdate_kernel(int n4, float* __restrict__ d, float* __restrict__ p,
                                                                   const float* __restrict__ r,
                                                                   const float* __restrict__ J, CgState* in) {
-    if (*(volatile uint32_t*)&in->done) return;
+    const uint32_t k = *(volatile uint32_t*)&in->k;
+    if (*(volatile uint32_t*)&in->xTag == k) return;
+    const bool last = *(volatile uint32_t*)&in->done != 0u;
+    const float alpha = (float)in->alpha;
     const float beta = (float)in->beta;
     const int n4q = n4 >> 2;
+    float4* d4 = reinterpret_cast<float4*>(d);
     float4* p4 = reinterpret_cast<float4*>(p);
     const float4* r4 = reinterpret_cast<const float4*>(r);
     const float4* j4 = reinterpret_cast<const float4*>(J);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4q; i += gridDim.x * blockDim.x) {
-        float4 pv = p4[i];
-        const float4 rv = r4[i], jv = j4[i];
-        pv.x = fmaf(beta, pv.x, rv.x * jv.x);
-        pv.y = fmaf(beta, pv.y, rv.y * jv.y);
-        pv.z = fmaf(beta, pv.z, rv.z * jv.z);
-        pv.w = fmaf(beta, pv.w, rv.w * jv.w);
-        p4[i] = pv;
+        float4 dv = d4[i], pv = p4[i];
+        dv.x = fmaf(alpha, pv.x, dv.x);
+        dv.y = fmaf(alpha, pv.y, dv.y);
+        dv.z = fmaf(alpha, pv.z, dv.z);
+        dv.w = fmaf(alpha, pv.w, dv.w);
+        d4[i] = dv;
+        if (!last) {
+            const float4 rv = r4[i], jv = j4[i];
+            pv.x = fmaf(beta, pv.x, rv.x * jv.x);
+            pv.y = fmaf(beta, pv.y, rv.y * jv.y);
+            pv.z = fmaf(beta, pv.z, rv.z * jv.z);
+            pv.w = fmaf(beta, pv.w, rv.w * jv.w);
+            p4[i] = pv;
+        }
+    }
+    __shared__ bool amLast;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        amLast = atomicAdd(&in->counters[3], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (amLast && threadIdx.x == 0) {
+        in->counters[3] = 0u;
+        in->xTag = k;
     }
 }
 
@@ -223,14 +241,14 @@ cudaError_t ir_inner_init_launch(int grid, cudaStream_t s, int n4, const double*
                                                       innerTol);
     return cudaGetLastError();
 }
-cudaError_t cg32_update_launch(int grid, cudaStream_t s, int n4, float* d, float* r, const float* p, const float* Ap,
-                               const float* J, CgState* in, double* partials, uint64_t innerHandle, int useCond) {
-    cg32_update_kernel<<<grid, kMxThreads, 0, s>>>(n4, d, r, p, Ap, J, in, partials, innerHandle, useCond);
+cudaError_t cg32_update_launch(int grid, cudaStream_t s, int n4, float* r, const float* Ap, const float* J,
+                               CgState* in, double* partials, uint64_t innerHandle, int useCond) {
+    cg32_update_kernel<<<grid, kMxThreads, 0, s>>>(n4, r, Ap, J, in, partials, innerHandle, useCond);
     return cudaGetLastError();
 }
-cudaError_t cg32_pupdate_launch(int grid, cudaStream_t s, int n4, float* p, const float* r, const float* J,
+cudaError_t cg32_pupdate_launch(int grid, cudaStream_t s, int n4, float* d, float* p, const float* r, const float* J,
                                 CgState* in) {
-    cg32_pupdate_kernel<<<grid, kMxThreads, 0, s>>>(n4, p, r, J, in);
+    cg32_pupdate_kernel<<<grid, kMxThreads, 0, s>>>(n4, d, p, r, J, in);
     return cudaGetLastError();
 }
 cudaError_t ir_update_launch(int grid, cudaStream_t s, int n4, double* x, const float* d, CgState* st,

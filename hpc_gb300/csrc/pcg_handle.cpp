@@ -275,22 +275,51 @@ void PcgHandle::refreshSellValues() {
           "sliced fill");
 }
 
-int PcgHandle::numSpmvCfgs() const { return spmv_num_configs() + sell_num_configs(); }
+// Configuration index space: [0, ncsr) staged CSR shapes, [ncsr, ncsr +
+// nsell) sliced unroll depths, ncsr + nsell the merge-path kernel.
+int PcgHandle::numSpmvCfgs() const { return spmv_num_configs() + sell_num_configs() + 1; }
 
-bool PcgHandle::isSell(int cfg) const { return cfg >= spmv_num_configs(); }
+bool PcgHandle::isSell(int cfg) const {
+    return cfg >= spmv_num_configs() && cfg < spmv_num_configs() + sell_num_configs();
+}
+
+bool PcgHandle::isMerge(int cfg) const { return cfg == spmv_num_configs() + sell_num_configs(); }
+
+void PcgHandle::ensureMergeScratch() {
+    const int nt = merge_tiles((int)m_n, (int64_t)m_nnz);
+    alloc(m_mergeRow, sizeof(int) * ((size_t)nt + 1), "merge carries");
+    alloc(m_mergeVal, sizeof(double) * ((size_t)nt + 1), "merge carries");
+    alloc(m_mergePart, sizeof(double) * ((size_t)nt + merge_fixup_grid(nt) + 1), "merge partials");
+}
 
 int PcgHandle::spmvGrid64(int cfg) {
+    if (isMerge(cfg)) {
+        ensureMergeScratch();
+        return merge_tiles((int)m_n, (int64_t)m_nnz);
+    }
     if (!isSell(cfg)) return spmv_grid<double>(cfg, (int)m_n, m_numSms);
     return ensureSell() ? sell_grid<double>(cfg - spmv_num_configs(), (int)m_n, m_numSms) : 0;
 }
 
 int PcgHandle::spmvGrid32(int cfg) {
+    if (isMerge(cfg)) {
+        ensureMergeScratch();
+        return merge_tiles((int)m_n, (int64_t)m_nnz);
+    }
     if (!isSell(cfg)) return spmv_grid<float>(cfg, (int)m_n, m_numSms);
     return sell_grid<float>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
 }
 
 cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, const double* b, CgState* st,
                               double* part, int mode, const uint32_t* done) {
+    if (isMerge(cfg)) {
+        const int m = mode == kSpmvResidual ? kSpmvPlain : mode;
+        cudaError_t e = spmv_merge_launch<double>(m_stream, (int)m_n, (int)m_nnz, m_rowptr.as<int>(), m_col.as<int>(),
+                                                  m_val.as<double>(), x, y, m_mergeRow.as<int>(), m_mergeVal.p,
+                                                  m_mergePart.as<double>(), st, m, done);
+        if (e != cudaSuccess || mode != kSpmvResidual) return e;
+        return residual_finish_launch<double>(m_stream, (int)m_n, b, y, part, st);
+    }
     if (!isSell(cfg))
         return spmv_launch<double>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
                                    m_val.as<double>(), x, y, b, st, part, mode, done);
@@ -300,6 +329,10 @@ cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, con
 
 cudaError_t PcgHandle::spmv32(int cfg, int grid, const float* x, float* y, const float* b, CgState* st,
                               double* part, int mode, const uint32_t* done) {
+    if (isMerge(cfg))  // the fp32 inner loop only uses the kCgDot mode
+        return spmv_merge_launch<float>(m_stream, (int)m_n, (int)m_nnz, m_rowptr.as<int>(), m_col.as<int>(),
+                                        m_val32.as<float>(), x, y, m_mergeRow.as<int>(), m_mergeVal.p,
+                                        m_mergePart.as<double>(), st, mode, done);
     if (!isSell(cfg))
         return spmv_launch<float>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
                                   m_val32.as<float>(), x, y, b, st, part, mode, done);
@@ -342,6 +375,8 @@ void PcgHandle::tuneSpmv() {
     const int forcedCfg = envInt("XJPCG_SPMV_CFG", -1);
     if (forcedCfg >= 0 && forcedCfg < ncfg) {
         best = forcedCfg;
+    } else if (m_forcedLanes == -2) {
+        best = spmv_num_configs() + sell_num_configs();
     } else if (m_forcedLanes < 0) {
         if (!ensureSell()) throw InvalidValue("the sliced SpMV layout is not available for this matrix.");
         best = spmv_num_configs();
@@ -448,10 +483,9 @@ void PcgHandle::buildGraph() {
     check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part, kSpmvCgDot,
                               &st->done),
           "SpMV kernel");
-    check(cg_update_launch(vg, m_stream, n4, m_x.as<double>(), m_r.as<double>(), m_p.as<double>(),
-                           m_Ap.as<double>(), m_J.as<double>(), st, part),
+    check(cg_update_launch(vg, m_stream, n4, m_r.as<double>(), m_Ap.as<double>(), m_J.as<double>(), st, part),
           "update kernel");
-    check(cg_pupdate_launch(vg, m_stream, n4, m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
+    check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
           "p kernel");
     check(cudaStreamEndCapture(m_stream, &body), "capture body end");
     check(cudaGraphInstantiate(&m_exec, g, 0), "graph instantiate");
@@ -498,10 +532,9 @@ Results PcgHandle::run(uint32_t maxIter, double tol) {
                 check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part,
                                           kSpmvCgDot, &st->done),
                       "SpMV kernel");
-                check(cg_update_launch(vg, m_stream, n4, m_x.as<double>(), m_r.as<double>(), m_p.as<double>(),
-                                       m_Ap.as<double>(), m_J.as<double>(), st, part),
+                check(cg_update_launch(vg, m_stream, n4, m_r.as<double>(), m_Ap.as<double>(), m_J.as<double>(), st, part),
                       "update kernel");
-                check(cg_pupdate_launch(vg, m_stream, n4, m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
+                check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
                       "p kernel");
             }
             ran += 16;
@@ -615,10 +648,11 @@ void PcgHandle::buildMixedGraph() {
           "capture");
     check(spmv32(cfg32, grid32, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, in, part, kSpmvCgDot, &in->done),
           "SpMV fp32");
-    check(cg32_update_launch(vg, m_stream, n4, m_d32.as<float>(), m_r32.as<float>(), m_p32.as<float>(),
-                             m_Ap32.as<float>(), m_J32.as<float>(), in, part, (uint64_t)m_condInner, 1),
+    check(cg32_update_launch(vg, m_stream, n4, m_r32.as<float>(), m_Ap32.as<float>(), m_J32.as<float>(), in, part,
+                             (uint64_t)m_condInner, 1),
           "update fp32");
-    check(cg32_pupdate_launch(vg, m_stream, n4, m_p32.as<float>(), m_r32.as<float>(), m_J32.as<float>(), in),
+    check(cg32_pupdate_launch(vg, m_stream, n4, m_d32.as<float>(), m_p32.as<float>(), m_r32.as<float>(),
+                              m_J32.as<float>(), in),
           "p fp32");
     check(cudaStreamEndCapture(m_stream, &innerBody), "capture end");
     // outer body part 2: x update after the inner loop
@@ -949,7 +983,13 @@ int PcgHandle::tuning(float* ms, int* shape, int cap) const {
     const int ncfg = numSpmvCfgs();
     for (int c = 0; c < ncfg && c < cap; ++c) {
         ms[c] = c < (int)m_tuneMs.size() ? m_tuneMs[c] : -1.f;
-        if (isSell(c)) {
+        if (isMerge(c)) {
+            // merge path: lanes 0, 256 threads, 8 path steps per thread
+            shape[4 * c] = 0;
+            shape[4 * c + 1] = 256;
+            shape[4 * c + 2] = 8;
+            shape[4 * c + 3] = 0;
+        } else if (isSell(c)) {
             // sliced layout: one lane per row, no CTA staging; chunk = unroll
             shape[4 * c] = 1;
             shape[4 * c + 1] = 0;
@@ -968,8 +1008,8 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->n4 = m_n4;
     info->nnz = m_nnz;
     info->itersRun = m_lastState.k;
-    info->spmvLanes = isSell(m_spmvCfg) ? 1u : (uint32_t)spmv_config_lanes(m_spmvCfg);
-    info->spmvLayout = isSell(m_spmvCfg) ? 1u : 0u;
+    info->spmvLanes = isMerge(m_spmvCfg) ? 0u : (isSell(m_spmvCfg) ? 1u : (uint32_t)spmv_config_lanes(m_spmvCfg));
+    info->spmvLayout = isMerge(m_spmvCfg) ? 2u : (isSell(m_spmvCfg) ? 1u : 0u);
     info->spmvGrid = (uint32_t)m_spmvGrid;
     info->statusBits = m_lastState.status;
     info->outerSweeps = m_lastOuter;

@@ -124,6 +124,8 @@ class PcgHandle {
     void tuneSpmv();
     int numSpmvCfgs() const;
     bool isSell(int cfg) const;
+    bool isMerge(int cfg) const;
+    void ensureMergeScratch();
     int spmvGrid64(int cfg);
     int spmvGrid32(int cfg);
     bool ensureSell();
@@ -160,6 +162,7 @@ class PcgHandle {
     // sliced (SELL-32) copy of the matrix, built on demand by the tuner
     DevBuf m_sliceOff, m_sellCol, m_sellVal, m_sellVal32;
     int m_sellState = 0;  // 0 not built, 1 built, 2 rejected (too much padding)
+    DevBuf m_mergeRow, m_mergeVal, m_mergePart;  // merge-path carries and partials
     int64_t m_sellTotal = 0;
     bool m_sell32Valid = false;
     bool m_val32Valid = false;

@@ -38,14 +38,26 @@ cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const in
                              const VT* sval, const VT* x, VT* y, const VT* b, CgState* state, double* partials,
                              int mode, const uint32_t* doneFlag);
 
+// ---- merge-path SpMV (spmv_merge.cu) ----
+// Scratch per matrix: carryRow[ntiles] ints, carryVal[ntiles] accumulators
+// (double for fp64, float for fp32), partials[ntiles + merge_fixup_grid(ntiles)].
+int merge_tiles(int n, int64_t nnz);
+int merge_fixup_grid(int ntiles);
+template <typename VT>
+cudaError_t spmv_merge_launch(cudaStream_t st, int n, int nnz, const int* rowptr, const int* col, const VT* val,
+                              const VT* x, VT* y, int* carryRow, void* carryVal, double* partials, CgState* state,
+                              int mode, const uint32_t* doneFlag);
+template <typename VT>
+cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, double* partials, CgState* state);
+
 // ---- CG vector kernels (cg_kernels.cu) ----
 int vec_grid(int n4, int numSms);
 cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x,
                            double* r, double* p, double* J, double* Ap, CgState* state, double* partials);
-cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* x, double* r, const double* p,
-                             const double* Ap, const double* J, CgState* state, double* partials);
-cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* p, const double* r, const double* J,
-                              CgState* state);
+cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, const double* Ap, const double* J,
+                             CgState* state, double* partials);
+cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* r,
+                              const double* J, CgState* state);
 
 // ---- mixed precision (mixed_kernels.cu) ----
 cudaError_t ir_init_launch(int grid, cudaStream_t s, int n, int n4, const double* b, const double* diag, double* x,
@@ -54,9 +66,9 @@ cudaError_t ir_check_launch(cudaStream_t s, CgState* st, CgState* in, uint64_t o
 cudaError_t ir_inner_init_launch(int grid, cudaStream_t s, int n4, const double* r64, const float* J32, float* r32,
                                  float* p32, float* d32, CgState* st, CgState* in, double* partials,
                                  uint64_t innerHandle, double innerTol);
-cudaError_t cg32_update_launch(int grid, cudaStream_t s, int n4, float* d, float* r, const float* p, const float* Ap,
-                               const float* J, CgState* in, double* partials, uint64_t innerHandle, int useCond);
-cudaError_t cg32_pupdate_launch(int grid, cudaStream_t s, int n4, float* p, const float* r, const float* J,
+cudaError_t cg32_update_launch(int grid, cudaStream_t s, int n4, float* r, const float* Ap, const float* J,
+                               CgState* in, double* partials, uint64_t innerHandle, int useCond);
+cudaError_t cg32_pupdate_launch(int grid, cudaStream_t s, int n4, float* d, float* p, const float* r, const float* J,
                                 CgState* in);
 cudaError_t ir_update_launch(int grid, cudaStream_t s, int n4, double* x, const float* d, CgState* st,
                              const CgState* in);

@@ -42,7 +42,7 @@ struct alignas(16) CgState {
     uint32_t useCond;              // 1 when running under a conditional node
     uint32_t outer;                // mixed precision: refinement sweeps
     uint32_t innerK;               // mixed precision: inner iterations total
-    uint32_t pad;
+    uint32_t xTag;                 // iteration whose x update has been applied
 };
 
 }  // namespace xjpcg

@@ -161,34 +161,39 @@ def zipf_spd(n: int = 2_000_000, alpha: float = 1.8, lo: int = 4, hi: int = 4096
     d_i = 10^U(-3, 3); b ~ U[-1, 1].  A0 = W + diag(1.01 sum_j |w_ij|),
     A = D A0 D with D = diag(d).
     """
+    import scipy.sparse as sps
+
     rng = np.random.default_rng(seed)
     L = np.clip(rng.zipf(alpha, n), lo, hi).astype(np.int64)
     rows = np.repeat(np.arange(n, dtype=np.int64), L)
     cols = rng.integers(0, n, size=int(L.sum()), dtype=np.int64)
     keep = rows != cols
-    a = np.minimum(rows, cols)[keep]
-    bcol = np.maximum(rows, cols)[keep]
+    key = np.minimum(rows, cols)[keep] * n + np.maximum(rows, cols)[keep]
     del rows, cols, keep
-    key = np.unique(a * n + bcol)
-    del a, bcol
+    key = np.sort(key)  # sorted distinct pairs (np.unique is much slower here)
+    first = np.empty(key.size, bool)
+    first[:1] = True
+    np.not_equal(key[1:], key[:-1], out=first[1:])
+    key = key[first]
+    del first
     pa = key // n
-    pb = key % n
+    pb = key - pa * n
     del key
     w = rng.standard_normal(pa.size)
     d = 10.0 ** rng.uniform(-3.0, 3.0, n)
-    absrow = np.bincount(pa, np.abs(w), minlength=n) + np.bincount(pb, np.abs(w), minlength=n)
-    diag0 = 1.01 * absrow
+    absw = np.abs(w)
+    diag0 = 1.01 * (np.bincount(pa, absw, minlength=n) + np.bincount(pb, absw, minlength=n))
     diag0[diag0 == 0] = 1.0
-    r = np.concatenate([pa, pb, np.arange(n, dtype=np.int64)])
-    c = np.concatenate([pb, pa, np.arange(n, dtype=np.int64)])
-    v = np.concatenate([w, w, diag0])
+    ar = np.arange(n, dtype=np.int64)
+    A = sps.csr_matrix((np.concatenate([w, w, diag0]),
+                        (np.concatenate([pa, pb, ar]), np.concatenate([pb, pa, ar]))), shape=(n, n))
     del pa, pb, w
-    order = np.argsort(r * n + c, kind="stable")
-    r, c, v = r[order], c[order], v[order]
-    del order
-    v = v * d[r] * d[c]
-    rowptr = np.zeros(n + 1, np.int64)
-    np.cumsum(np.bincount(r, minlength=n), out=rowptr[1:])
+    A.sort_indices()
+    rowptr = A.indptr.astype(np.int64)
+    c = A.indices.astype(np.int64)
+    r = np.repeat(ar, np.diff(rowptr))
+    v = A.data * d[r] * d[c]
+    del A, r
     diag = diag0 * d * d
     b = rng.uniform(-1.0, 1.0, n)
     return System(n, rowptr.astype(np.int32), c.astype(np.int32), v, diag, b, "zipf_spd_%d" % n)

@@ -12,6 +12,8 @@ per case, the inputs and what the reference produced:
                              and ordered (row, partition, position)
   sig_sha256                 SHA-256 of each signature file (rbParam, parParam,
                              info, nnzVal_0..15), for a byte-level exporter
+  sig_raw_<file>             the signature files' bytes, for the cases whose
+                             padded size is at most RAW_MAX_PADDED entries
   sig2_*                     the same after the values-only update
                              (updateMat / updateCscSymMat) when the case has one
 
@@ -111,6 +113,9 @@ def _csc_cases():
     return cases
 
 
+RAW_MAX_PADDED = 40000
+
+
 def _sha(path):
     out = {}
     for f in sorted(os.listdir(path)):
@@ -130,6 +135,12 @@ def _store_sig(prefix, path, rec):
     rec[prefix + "_padded"] = np.int64(dec["val"].size)
     sha = _sha(path)
     rec[prefix + "_sha256"] = np.array(["%s=%s" % kv for kv in sorted(sha.items())])
+    if dec["val"].size <= RAW_MAX_PADDED:
+        # raw signature bytes of the small cases, for the device-side decoder
+        # and the byte-level exporter tests
+        for f in sorted(os.listdir(path)):
+            with open(os.path.join(path, f), "rb") as fh:
+                rec[prefix + "_raw_" + f.replace(".dat", "")] = np.frombuffer(fh.read(), np.uint8)
 
 
 def run(reference_root="/root/reference"):

@@ -45,7 +45,7 @@ def test_diffusion27_small_csr(handle):
     _check_solve(s, r)
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32, -1])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32, -1, -2])
 def test_every_spmv_shape_solves(handle, lanes):
     s = W.diffusion27(12, sigma=1.5, seed=7)
     rows, cols, vals = s.coo()
@@ -55,7 +55,7 @@ def test_every_spmv_shape_solves(handle, lanes):
     if lanes > 0:
         assert handle.info().spmvLanes == lanes and handle.info().spmvLayout == 0
     else:
-        assert handle.info().spmvLayout == 1
+        assert handle.info().spmvLayout == (1 if lanes == -1 else 2)
     _check_solve(s, r)
 
 
@@ -107,7 +107,7 @@ def test_conversion_long_rows(handle):
     orp, oci, opm = oracle.coo_to_csr(n, rows, cols)
     assert np.array_equal(rp, orp) and np.array_equal(ci, oci) and np.array_equal(pm, opm)
     x = rng.standard_normal(n)
-    for lanes in [1, 4, 32]:
+    for lanes in [1, 4, 32, -2]:
         handle.set_spmv_lanes(lanes)
         y = handle.spmv(x)
         yref = oracle.spmv(orp, oci, vals[opm], x)
@@ -138,7 +138,7 @@ def test_cscsym_bitexact(handle):
         _check_solve(s, res, max_iter=2000)
 
 
-@pytest.mark.parametrize("lanes", [0, 1, 2, 4, 8, 16, 32, -1])
+@pytest.mark.parametrize("lanes", [0, 1, 2, 4, 8, 16, 32, -1, -2])
 def test_spmv_matches_oracle(handle, lanes):
     s = W.diffusion27(24, seed=5)
     rows, cols, vals = s.coo()
@@ -298,6 +298,25 @@ def test_zero_rhs_breakdown(handle):
     # running to maxIter on NaN.
     assert r.status == X.EXECUTION_FAILED
     assert handle.info().itersRun == 1
+
+
+@pytest.mark.parametrize("lanes", [0, -2])
+def test_power_law_rows_merge_path(handle, lanes):
+    """Zipf rows (4 .. 4096+ entries): SpMV and a solve with the merge-path
+    kernel against the oracle."""
+    s = W.zipf_spd(60000, seed=5)
+    r = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 0, 1e-10)
+    handle.set_spmv_lanes(lanes)
+    x = np.random.default_rng(4).standard_normal(s.n)
+    y = handle.spmv(x)
+    yref = oracle.spmv(s.rowptr, s.col, s.val, x)
+    scale = oracle.spmv(s.rowptr, s.col, np.abs(s.val), np.abs(x))
+    assert np.all(np.abs(y - yref) <= 1e-13 * scale)
+    r = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    _check_solve(s, r)
+    m = handle.mixed_solve(s.b, s.diag, 20000, 1e-10)
+    assert m.status == X.SUCCESS, m.message
+    assert oracle.true_relres(s.rowptr, s.col, s.val, s.b, m.x) <= 1.5e-10
 
 
 def test_mixed_precision_small(handle):
