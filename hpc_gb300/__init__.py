@@ -37,7 +37,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbCsrSolver", "xJPCG_gbSolveDevice", "xJPCG_gbMixedSolve", "xJPCG_gbSpmv", "xJPCG_gbGetCsr",
     "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes",
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
-    "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad",
+    "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv",
 ]
 
 
@@ -114,6 +114,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
     lib.xJPCG_gbAdjointSolve.argtypes = [_P, _P, _P, _P, _P, u32, dbl, C.POINTER(u32), C.POINTER(dbl), C.c_int]
     lib.xJPCG_gbEdgeGrad.argtypes = [_P, i64, _P, _P, _P, _P, C.c_int]
+    lib.xJPCG_gbSetSignatureMatrix.argtypes = [_P, u32, _P, _P, _P, u64, _P, u64]
+    lib.xJPCG_gbSignatureSpmv.argtypes = [_P, _P, u32, _P, u32, u32, _P, u64]
     lib.xJPCG_gbBatchSolve.argtypes = [_P, u32, _P, _P, _P, _P, _P, _P, _P, u32, dbl, C.c_int, _P, C.c_int]
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
@@ -320,6 +322,32 @@ class JPCG:
                                          _ptr(diag), _ptr(b), _ptr(x), max_iter, tol, precision, _ptr(res), 0)
         xs = [x[sys_row[i]:sys_row[i + 1]] for i in range(len(systems))]
         return st, xs, res
+
+    def set_signature_matrix(self, nnz_bufs, par_param, rb_param):
+        """Loads the reference's partitioned-matrix buffers (16 nnzVal channel
+        buffers, parParam, rbParam as numpy uint8 arrays)."""
+        bufs = [np.ascontiguousarray(b, np.uint8) for b in nnz_bufs]
+        ptrs = (C.c_void_p * len(bufs))(*[b.ctypes.data for b in bufs])
+        sizes = (C.c_uint64 * len(bufs))(*[b.size for b in bufs])
+        par = np.ascontiguousarray(par_param, np.uint8)
+        rb = np.ascontiguousarray(rb_param, np.uint8)
+        st = self.lib.xJPCG_gbSetSignatureMatrix(self.h, len(bufs), C.cast(ptrs, C.c_void_p), C.cast(sizes, C.c_void_p),
+                                                 _ptr(par), par.size, _ptr(rb), rb.size)
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        self._sig_keep = (bufs, par, rb)
+
+    def signature_spmv(self, x, y_rows, start_addr=0, frame=False):
+        """y = A x on the partitioned matrix; optionally the transY frame."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(y_rows, np.float64)
+        fb = 64 + 64 * max(1, (y_rows + 7) // 8)
+        fr = np.zeros(fb, np.uint8) if frame else None
+        st = self.lib.xJPCG_gbSignatureSpmv(self.h, _ptr(x), x.size, _ptr(y), y_rows, start_addr, _ptr(fr),
+                                            fb if frame else 0)
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        return (y, fr) if frame else y
 
     def spmv_tuning(self):
         """[(lanes, consumers, chunk, stages, ms)] of the last SpMV tuning."""

@@ -3,21 +3,15 @@
 // Per iteration the loop runs three launches (captured once in a CUDA graph,
 // inside a conditional WHILE node):
 //   1. SpMV + p.Ap + alpha            (spmv_kernels.cu, mode kCgDot)
-//   2. cg_update_kernel: r -= alpha Ap, z = J r (not stored), r.r and r.z
-//      reduced over the grid; the last CTA forms beta, writes the 64-byte
-//      iteration record, applies the stop rule and sets the loop's
-//      condition.  This fuses the reference's krnl_update_rk_jacobi
+//   2. cg_update_kernel: x += alpha p, r -= alpha Ap, z = J r (not stored),
+//      r.r and r.z reduced over the grid; the last CTA forms beta, writes the
+//      64-byte iteration record, applies the stop rule and sets the loop's
+//      condition.  This fuses the reference's krnl_update_xk (L1/hpc/include/
+//      hw/cgSolver/update_xk.hpp:26-67), krnl_update_rk_jacobi
 //      (update_rk_jacobi.hpp:29-110) and krnl_control (pcg/hw/include/
 //      control.hpp:65-92, tasks.hpp:43-47).
-//   3. cg_pupdate_kernel: x += alpha p (krnl_update_xk, L1/hpc/include/hw/
-//      cgSolver/update_xk.hpp:26-67), then p = z + beta p with z = J r
-//      recomputed (update_pk.hpp:26-72).  Doing the x update here, where p is
-//      read anyway, saves one read of p per iteration (80 n bytes of vector
-//      traffic instead of 88 n) with identical arithmetic: x_{k+1} = x_k +
-//      alpha_k p_k uses the same alpha_k and the same (not yet updated) p_k.
-//      It runs on the last iteration too (only the p part is skipped), and a
-//      per-iteration tag keeps a relaunch in the host-driven loop from
-//      applying it twice.
+//   3. cg_pupdate_kernel: p = z + beta p with z = J r recomputed
+//      (update_pk.hpp:26-72).
 // The vector init kernel restates GenCgVector::init (pcg/sw/include/impl/
 // cgVector.hpp:101-114) and the instruction slot 0 (cgVector.hpp:149-159).
 // Reductions are fixed-order (per-CTA tree, then the last CTA sums the CTA
@@ -76,7 +70,6 @@ __global__ void __launch_bounds__(kVecThreads) cg_init_kernel(int n, int n4, con
         s->rr = fin[0];
         s->tols = fin[0] * s->tol * s->tol;
         s->k = 0;
-        s->xTag = 0;
         s->done = 0;
         s->status &= ~(kStatusBreakdown | kStatusWaitTimeout);
         s->vecSize = (uint32_t)n4;
@@ -93,7 +86,8 @@ __global__ void __launch_bounds__(kVecThreads) cg_init_kernel(int n, int n4, con
     }
 }
 
-__global__ void __launch_bounds__(kVecThreads) cg_update_kernel(int n4, double* __restrict__ r,
+__global__ void __launch_bounds__(kVecThreads) cg_update_kernel(int n4, double* __restrict__ x, double* __restrict__ r,
+                                                                const double* __restrict__ p,
                                                                 const double* __restrict__ Ap,
                                                                 const double* __restrict__ J, CgState* state,
                                                                 double* partials) {
@@ -107,12 +101,16 @@ __global__ void __launch_bounds__(kVecThreads) cg_update_kernel(int n4, double* 
     const double alpha = state->alpha;
     double rr = 0.0, rz = 0.0;
     const int n2 = n4 >> 1;
+    double2* x2 = reinterpret_cast<double2*>(x);
     double2* r2 = reinterpret_cast<double2*>(r);
+    const double2* p2 = reinterpret_cast<const double2*>(p);
     const double2* a2 = reinterpret_cast<const double2*>(Ap);
     const double2* j2 = reinterpret_cast<const double2*>(J);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
-        double2 rv = r2[i];
-        const double2 av = __ldcs(&a2[i]), jv = j2[i];
+        double2 xv = x2[i], rv = r2[i];
+        const double2 pv = p2[i], av = __ldcs(&a2[i]), jv = j2[i];
+        xv.x = fma(alpha, pv.x, xv.x);
+        xv.y = fma(alpha, pv.y, xv.y);
         rv.x = fma(-alpha, av.x, rv.x);
         rv.y = fma(-alpha, av.y, rv.y);
         const double z0 = rv.x * jv.x, z1 = rv.y * jv.y;
@@ -120,6 +118,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_update_kernel(int n4, double* 
         rr = fma(rv.y, rv.y, rr);
         rz = fma(rv.x, z0, rz);
         rz = fma(rv.y, z1, rz);
+        x2[i] = xv;
         r2[i] = rv;
     }
     double v[2] = {rr, rz};
@@ -148,53 +147,21 @@ __global__ void __launch_bounds__(kVecThreads) cg_update_kernel(int n4, double* 
     }
 }
 
-__global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double* __restrict__ x,
-                                                                 double* __restrict__ p,
+__global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double* __restrict__ p,
                                                                  const double* __restrict__ r,
                                                                  const double* __restrict__ J, CgState* state) {
-    // state->k counts the iterations whose update kernel ran; state->xTag is
-    // the iteration whose x update is applied.  Equal tags: nothing pending.
-    const uint32_t k = *(volatile uint32_t*)&state->k;
-    if (*(volatile uint32_t*)&state->xTag == k) return;
-    const bool last = *(volatile uint32_t*)&state->done != 0u;
-    const double alpha = state->alpha;
+    if (*(volatile uint32_t*)&state->done) return;
     const double beta = state->beta;
     const int n2 = n4 >> 1;
-    double2* x2 = reinterpret_cast<double2*>(x);
     double2* p2 = reinterpret_cast<double2*>(p);
     const double2* r2 = reinterpret_cast<const double2*>(r);
     const double2* j2 = reinterpret_cast<const double2*>(J);
-    if (last) {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
-            double2 xv = x2[i];
-            const double2 pv = p2[i];
-            xv.x = fma(alpha, pv.x, xv.x);
-            xv.y = fma(alpha, pv.y, xv.y);
-            x2[i] = xv;
-        }
-    } else {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
-            double2 xv = x2[i], pv = p2[i];
-            const double2 rv = r2[i], jv = j2[i];
-            xv.x = fma(alpha, pv.x, xv.x);
-            xv.y = fma(alpha, pv.y, xv.y);
-            pv.x = fma(beta, pv.x, rv.x * jv.x);
-            pv.y = fma(beta, pv.y, rv.y * jv.y);
-            x2[i] = xv;
-            p2[i] = pv;
-        }
-    }
-    // The last CTA to finish marks iteration k's x update as applied.
-    __shared__ bool amLast;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        amLast = atomicAdd(&state->counters[3], 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (amLast && threadIdx.x == 0) {
-        state->counters[3] = 0u;
-        state->xTag = k;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        double2 pv = p2[i];
+        const double2 rv = r2[i], jv = j2[i];
+        pv.x = fma(beta, pv.x, rv.x * jv.x);
+        pv.y = fma(beta, pv.y, rv.y * jv.y);
+        p2[i] = pv;
     }
 }
 
@@ -211,15 +178,15 @@ cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const doubl
     return cudaGetLastError();
 }
 
-cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, const double* Ap, const double* J,
-                             CgState* state, double* partials) {
-    cg_update_kernel<<<grid, kVecThreads, 0, st>>>(n4, r, Ap, J, state, partials);
+cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* x, double* r, const double* p,
+                             const double* Ap, const double* J, CgState* state, double* partials) {
+    cg_update_kernel<<<grid, kVecThreads, 0, st>>>(n4, x, r, p, Ap, J, state, partials);
     return cudaGetLastError();
 }
 
-cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* r,
-                              const double* J, CgState* state) {
-    cg_pupdate_kernel<<<grid, kVecThreads, 0, st>>>(n4, x, p, r, J, state);
+cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* p, const double* r, const double* J,
+                              CgState* state) {
+    cg_pupdate_kernel<<<grid, kVecThreads, 0, st>>>(n4, p, r, J, state);
     return cudaGetLastError();
 }
 

@@ -303,6 +303,29 @@ XJPCG_Status_t xJPCG_gbMixedSolve(XJPCG_Handle_t* handle, const double* b, const
     XJ_GUARD_END("Solver returns successfully")
 }
 
+XJPCG_Status_t xJPCG_gbSetSignatureMatrix(XJPCG_Handle_t* handle, uint32_t numChannels, const void* const* nnzBufs,
+                                          const uint64_t* nnzBytes, const void* parParam, uint64_t parParamBytes,
+                                          const void* rbParam, uint64_t rbParamBytes) {
+    XJ_GUARD_BEGIN
+    auto last = std::chrono::high_resolution_clock::now();
+    if (nnzBufs == nullptr || nnzBytes == nullptr || parParam == nullptr || rbParam == nullptr)
+        throw xjpcg::InvalidValue("buffer is nullptr.");
+    p->setSignatureMatrix(numChannels, nnzBufs, nnzBytes, parParam, parParamBytes, rbParam, rbParamBytes);
+    p->markCalled();
+    p->metrics()->m_matProc = elapsed(last);
+    XJ_GUARD_END("Partitioned matrix loaded successfully")
+}
+
+XJPCG_Status_t xJPCG_gbSignatureSpmv(XJPCG_Handle_t* handle, const double* x, uint32_t xLen, double* y,
+                                     uint32_t yRows, uint32_t startAddr, void* frame, uint64_t frameBytes) {
+    XJ_GUARD_BEGIN
+    auto last = std::chrono::high_resolution_clock::now();
+    if (x == nullptr) throw xjpcg::InvalidValue("Vector is nullptr.");
+    p->signatureSpmv(x, xLen, y, yRows, startAddr, static_cast<unsigned char*>(frame), frameBytes);
+    p->metrics()->m_solver = elapsed(last);
+    XJ_GUARD_END("SpMV returns successfully")
+}
+
 XJPCG_Status_t xJPCG_gbAdjointSolve(XJPCG_Handle_t* handle, const double* g, const double* diagA, double* lambda,
                                     double* gradA, uint32_t maxIter, double tol, uint32_t* iter, double* res,
                                     int onDevice) {

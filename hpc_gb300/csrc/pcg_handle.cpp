@@ -483,9 +483,10 @@ void PcgHandle::buildGraph() {
     check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part, kSpmvCgDot,
                               &st->done),
           "SpMV kernel");
-    check(cg_update_launch(vg, m_stream, n4, m_r.as<double>(), m_Ap.as<double>(), m_J.as<double>(), st, part),
+    check(cg_update_launch(vg, m_stream, n4, m_x.as<double>(), m_r.as<double>(), m_p.as<double>(), m_Ap.as<double>(),
+                                       m_J.as<double>(), st, part),
           "update kernel");
-    check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
+    check(cg_pupdate_launch(vg, m_stream, n4, m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
           "p kernel");
     check(cudaStreamEndCapture(m_stream, &body), "capture body end");
     check(cudaGraphInstantiate(&m_exec, g, 0), "graph instantiate");
@@ -532,9 +533,10 @@ Results PcgHandle::run(uint32_t maxIter, double tol) {
                 check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part,
                                           kSpmvCgDot, &st->done),
                       "SpMV kernel");
-                check(cg_update_launch(vg, m_stream, n4, m_r.as<double>(), m_Ap.as<double>(), m_J.as<double>(), st, part),
+                check(cg_update_launch(vg, m_stream, n4, m_x.as<double>(), m_r.as<double>(), m_p.as<double>(), m_Ap.as<double>(),
+                                       m_J.as<double>(), st, part),
                       "update kernel");
-                check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
+                check(cg_pupdate_launch(vg, m_stream, n4, m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
                       "p kernel");
             }
             ran += 16;
@@ -583,20 +585,19 @@ void PcgHandle::buildMixedGraph() {
         m_mixedExec = nullptr;
     }
     const int n = (int)m_n, n4 = (int)m_n4;
+    (void)n;
     const int vg = vec_grid(n4, m_numSms);
     const int cfg32 = m_spmvCfg;
     const int grid32 = spmvGrid32(cfg32);
     CgState* st = m_state.as<CgState>();
-    CgState* in = m_state32.as<CgState>();
     double* part = m_partials.as<double>();
-    const double innerTol = envDouble("XJPCG_INNER_TOL", 1e-5);
     cudaGraph_t g = nullptr;
     check(cudaGraphCreate(&g, 0), "cudaGraphCreate");
     check(cudaStreamBeginCaptureToGraph(m_stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
           "capture");
-    check(ir_init_launch(vg, m_stream, n, n4, m_b.as<double>(), m_diag.as<double>(), m_x.as<double>(),
-                         m_J32.as<float>(), st, part),
-          "ir init");
+    check(rel_init_launch(vg, m_stream, (int)m_n, n4, m_b.as<double>(), m_diag.as<double>(), m_x.as<double>(),
+                          m_d32.as<float>(), m_J32.as<float>(), m_r32.as<float>(), m_p32.as<float>(), st, part),
+          "mixed init");
     check(cudaStreamEndCapture(m_stream, &g), "capture end");
     size_t nn = 0;
     check(cudaGraphGetNodes(g, nullptr, &nn), "nodes");
@@ -608,30 +609,25 @@ void PcgHandle::buildMixedGraph() {
     cp.conditional.handle = m_condOuter;
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
-    cudaGraphNode_t outerNode;
-    check(cudaGraphAddNode(&outerNode, g, nodes.data(), nullptr, nn, &cp), "outer node");
-    cudaGraph_t outerBody = cp.conditional.phGraph_out[0];
-
-    // outer body part 1: residual, check, inner init
-    check(cudaGraphConditionalHandleCreate(&m_condInner, outerBody, 0, 0), "handle");
-    check(cudaStreamBeginCaptureToGraph(m_stream, outerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+    cudaGraphNode_t loopNode;
+    check(cudaGraphAddNode(&loopNode, g, nodes.data(), nullptr, nn, &cp), "loop node");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    // body: FP32 SpMV + update, then IF refresh, then p update
+    check(cudaGraphConditionalHandleCreate(&m_condInner, body, 0, 0), "handle");
+    check(cudaStreamBeginCaptureToGraph(m_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
           "capture");
-    check(spmv64(m_spmvCfg, m_spmvGrid, m_x.as<double>(), m_r.as<double>(), m_b.as<double>(), st, part,
-                              kSpmvResidual, nullptr),
-          "residual SpMV");
-    check(ir_check_launch(m_stream, st, in, (uint64_t)m_condOuter, kMaxOuter), "ir check");
-    check(ir_inner_init_launch(vg, m_stream, n4, m_r.as<double>(), m_J32.as<float>(), m_r32.as<float>(),
-                               m_p32.as<float>(), m_d32.as<float>(), st, in, part, (uint64_t)m_condInner, innerTol),
-          "inner init");
-    check(cudaStreamEndCapture(m_stream, &outerBody), "capture end");
-    size_t on = 0;
-    check(cudaGraphGetNodes(outerBody, nullptr, &on), "nodes");
-    std::vector<cudaGraphNode_t> onodes(on);
-    check(cudaGraphGetNodes(outerBody, onodes.data(), &on), "nodes");
-    // The leaf of the outer body so far is the inner-init node: find nodes
-    // without dependents.
+    check(spmv32(cfg32, grid32, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, st, part, kSpmvCgDot, &st->done),
+          "SpMV fp32");
+    check(rel_update_launch(vg, m_stream, n4, m_d32.as<float>(), m_r32.as<float>(), m_p32.as<float>(),
+                            m_Ap32.as<float>(), m_J32.as<float>(), st, part),
+          "mixed update");
+    check(cudaStreamEndCapture(m_stream, &body), "capture end");
+    size_t bn = 0;
+    check(cudaGraphGetNodes(body, nullptr, &bn), "nodes");
+    std::vector<cudaGraphNode_t> bnodes(bn);
+    check(cudaGraphGetNodes(body, bnodes.data(), &bn), "nodes");
     std::vector<cudaGraphNode_t> leaves;
-    for (auto nd : onodes) {
+    for (auto nd : bnodes) {
         size_t cnt = 0;
         check(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &cnt), "deps");
         if (cnt == 0) leaves.push_back(nd);
@@ -639,27 +635,25 @@ void PcgHandle::buildMixedGraph() {
     cudaGraphNodeParams ip = {};
     ip.type = cudaGraphNodeTypeConditional;
     ip.conditional.handle = m_condInner;
-    ip.conditional.type = cudaGraphCondTypeWhile;
+    ip.conditional.type = cudaGraphCondTypeIf;
     ip.conditional.size = 1;
-    cudaGraphNode_t innerNode;
-    check(cudaGraphAddNode(&innerNode, outerBody, leaves.data(), nullptr, leaves.size(), &ip), "inner node");
-    cudaGraph_t innerBody = ip.conditional.phGraph_out[0];
-    check(cudaStreamBeginCaptureToGraph(m_stream, innerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+    cudaGraphNode_t ifNode;
+    check(cudaGraphAddNode(&ifNode, body, leaves.data(), nullptr, leaves.size(), &ip), "refresh node");
+    cudaGraph_t refresh = ip.conditional.phGraph_out[0];
+    check(cudaStreamBeginCaptureToGraph(m_stream, refresh, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
           "capture");
-    check(spmv32(cfg32, grid32, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, in, part, kSpmvCgDot, &in->done),
-          "SpMV fp32");
-    check(cg32_update_launch(vg, m_stream, n4, m_r32.as<float>(), m_Ap32.as<float>(), m_J32.as<float>(), in, part,
-                             (uint64_t)m_condInner, 1),
-          "update fp32");
-    check(cg32_pupdate_launch(vg, m_stream, n4, m_d32.as<float>(), m_p32.as<float>(), m_r32.as<float>(),
-                              m_J32.as<float>(), in),
+    check(rel_fold_launch(vg, m_stream, n4, m_x.as<double>(), m_d32.as<float>(), st), "fold");
+    check(spmv64(m_spmvCfg, m_spmvGrid, m_x.as<double>(), m_r.as<double>(), m_b.as<double>(), st, part,
+                 kSpmvResidual, nullptr),
+          "residual SpMV");
+    check(rel_restart_launch(vg, m_stream, n4, m_r.as<double>(), m_J32.as<float>(), m_r32.as<float>(), st, part),
+          "restart");
+    check(cudaStreamEndCapture(m_stream, &refresh), "capture end");
+    check(cudaStreamBeginCaptureToGraph(m_stream, body, &ifNode, nullptr, 1, cudaStreamCaptureModeThreadLocal),
+          "capture");
+    check(rel_pupdate_launch(vg, m_stream, n4, m_p32.as<float>(), m_r32.as<float>(), m_J32.as<float>(), st),
           "p fp32");
-    check(cudaStreamEndCapture(m_stream, &innerBody), "capture end");
-    // outer body part 2: x update after the inner loop
-    check(cudaStreamBeginCaptureToGraph(m_stream, outerBody, &innerNode, nullptr, 1, cudaStreamCaptureModeThreadLocal),
-          "capture");
-    check(ir_update_launch(vg, m_stream, n4, m_x.as<double>(), m_d32.as<float>(), st, in), "ir update");
-    check(cudaStreamEndCapture(m_stream, &outerBody), "capture end");
+    check(cudaStreamEndCapture(m_stream, &body), "capture end");
     check(cudaGraphInstantiate(&m_mixedExec, g, 0), "graph instantiate");
     cudaGraphDestroy(g);
     m_mixedGen = m_generation;
@@ -686,19 +680,18 @@ Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
               "sliced fp32 fill");
         m_sell32Valid = true;
     }
-    check(cudaMemsetAsync(m_p32.p, 0, vb32, m_stream), "memset");
     check(cudaMemsetAsync(m_Ap32.p, 0, vb32, m_stream), "memset");
     CgState* st = m_state.as<CgState>();
-    CgState* in = m_state32.as<CgState>();
+    buildMixedGraph();
     CgState cmd = {};
     cmd.tol = tol;
     cmd.maxIterP1 = maxIter + 1u;
     cmd.useCond = 1;
-    CgState cmdIn = {};
-    cmdIn.useCond = 1;
-    buildMixedGraph();
+    cmd.condHandle = (uint64_t)m_condOuter;
+    cmd.relHandle = (uint64_t)m_condInner;
+    const double delta = envDouble("XJPCG_RELIABLE_DELTA", 0.1);
+    cmd.delta2 = delta * delta;
     check(cudaMemcpyAsync(st, &cmd, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
-    check(cudaMemcpyAsync(in, &cmdIn, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
     check(cudaEventRecord(m_ev0, m_stream), "event");
     check(cudaGraphLaunch(m_mixedExec, m_stream), "graph launch");
     check(cudaEventRecord(m_ev1, m_stream), "event");
@@ -710,9 +703,9 @@ Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
     m_lastOuter = s.outer;
     m_lastInner = s.innerK;
     Results r;
-    r.itersRun = s.innerK;
-    r.reportedIters = s.innerK;
-    r.rrLast = s.rr;
+    r.itersRun = s.k;
+    r.reportedIters = s.k;
+    r.rrLast = s.rrTrue;
     r.bb = s.bb;
     r.status = s.status;
     m_lastBb = s.bb;
@@ -741,6 +734,171 @@ void PcgHandle::spmv(const double* x, double* y, bool onDevice) {
         check(cudaMemcpyAsync(y, dy, sizeof(double) * m_n, cudaMemcpyDeviceToHost, m_stream), "D2H y");
         check(cudaStreamSynchronize(m_stream), "sync");
     }
+}
+
+// ---------------------------------------------------------------------------
+// The reference's partitioned-matrix buffers (SpmvHost drop-in)
+// ---------------------------------------------------------------------------
+namespace {
+uint32_t rdU32(const unsigned char* p, uint64_t off) {
+    uint32_t v;
+    std::memcpy(&v, p + off, 4);
+    return v;
+}
+uint16_t rdU16(const unsigned char* p, uint64_t off) {
+    uint16_t v;
+    std::memcpy(&v, p + off, 2);
+    return v;
+}
+}  // namespace
+
+// Layouts: RowBlockParam (matrix_params.hpp:329-471): 32-byte header
+// {totalRows, totalRbs}, then per row block 8 x 32 bytes: {startRow, minCol,
+// cols, numPars}, {rows, nnzs}, u16[16] channel row offsets, u16[16]
+// channel rows, u32[16] channel nnzs, 32 bytes dummy.  ParParam (473-576):
+// 32-byte header {totalPars}, then per partition 8 x 32 bytes: u32[16]
+// channel columns, u32[16] channel nnzs, {baseColBlock, colBlocks, rows,
+// nnzs}, u16[16] channel column-block offsets, u16[16] channel column blocks,
+// dummy.  Chunks follow gen_nnzStore (signature.hpp:361-426).
+void PcgHandle::setSignatureMatrix(uint32_t nch, const void* const* bufs, const uint64_t* bytes, const void* par,
+                                   uint64_t parBytes, const void* rb, uint64_t rbBytes) {
+    if (nch != 16) throw InvalidValue("the partitioned format has 16 channels.");
+    const unsigned char* R = static_cast<const unsigned char*>(rb);
+    const unsigned char* P = static_cast<const unsigned char*>(par);
+    if (rbBytes < 32 || parBytes < 32) throw InvalidValue("parameter buffer too small.");
+    const uint32_t totalRows = rdU32(R, 0), totalRbs = rdU32(R, 4), totalPars = rdU32(P, 0);
+    if (32 + (uint64_t)totalRbs * 256 > rbBytes || 32 + (uint64_t)totalPars * 256 > parBytes)
+        throw InvalidValue("parameter buffer shorter than its header says.");
+    std::vector<uint64_t> chanOff(nch, 32), chanBase(nch, 0);
+    uint64_t totalBytes = 0;
+    for (uint32_t c = 0; c < nch; ++c) {
+        if (bufs[c] == nullptr || bytes[c] < 32) throw InvalidValue("channel buffer missing or too small.");
+        chanBase[c] = totalBytes;
+        totalBytes += (bytes[c] + 15) / 16 * 16;
+    }
+    std::vector<SigChunk> chunks;
+    int64_t groups = 0;
+    uint32_t maxColEnd = 0;
+    for (uint32_t p = 0; p < totalPars; ++p) {
+        const uint64_t pb = 32 + (uint64_t)p * 256;
+        maxColEnd = std::max(maxColEnd, (rdU32(P, pb + 128) + rdU32(P, pb + 132)) * 4u);
+    }
+    uint32_t parId = 0;
+    for (uint32_t r = 0; r < totalRbs; ++r) {
+        const uint64_t rbb = 32 + (uint64_t)r * 256;
+        const uint32_t startRow = rdU32(R, rbb), npars = rdU32(R, rbb + 12);
+        if ((uint64_t)parId + npars > totalPars) throw InvalidValue("row blocks reference missing partitions.");
+        for (uint32_t c = 0; c < nch; ++c) {
+            const int32_t rowBase = (int32_t)(startRow + rdU16(R, rbb + 64 + 2 * c));
+            for (uint32_t q = 0; q < npars; ++q) {
+                const uint64_t pb = 32 + (uint64_t)(parId + q) * 256;
+                const uint32_t chNnz = rdU32(P, pb + 64 + 4 * c);
+                if (chNnz % 32 != 0) throw InvalidValue("channel chunk is not a multiple of 32 entries.");
+                const int64_t ng = chNnz / 4;
+                if (ng == 0) continue;
+                const uint64_t chunkBytes = 32 * (uint64_t)(ng + (ng + 127) / 128 + (ng + 15) / 16);
+                if (chanOff[c] + chunkBytes > bytes[c]) throw InvalidValue("channel buffer shorter than its chunks.");
+                SigChunk ck;
+                ck.byteStart = (int64_t)(chanBase[c] + chanOff[c]);
+                ck.groupStart = groups;
+                ck.rowBase = rowBase;
+                ck.colBase = (int32_t)(rdU32(P, pb + 128) + rdU16(P, pb + 160 + 2 * c));
+                chunks.push_back(ck);
+                groups += ng;
+                chanOff[c] += chunkBytes;
+            }
+        }
+        parId += npars;
+    }
+    const uint32_t n = std::max(totalRows, maxColEnd);
+    if (n == 0 || groups == 0) throw InvalidValue("empty partitioned matrix.");
+    const int64_t entries = groups * 4;
+    if (entries > 0x7ffffff0ll) throw InvalidValue("partitioned matrix too large for int32 indexing.");
+    alloc(m_sigBuf, totalBytes + 16, "channel buffers");
+    for (uint32_t c = 0; c < nch; ++c)
+        check(cudaMemcpyAsync(m_sigBuf.as<unsigned char>() + chanBase[c], bufs[c], bytes[c], cudaMemcpyHostToDevice,
+                              m_stream),
+              "H2D channel");
+    alloc(m_sigChunks, sizeof(SigChunk) * chunks.size(), "chunk table");
+    check(cudaMemcpyAsync(m_sigChunks.p, chunks.data(), sizeof(SigChunk) * chunks.size(), cudaMemcpyHostToDevice,
+                          m_stream),
+          "H2D chunks");
+    alloc(m_sigRow, sizeof(uint32_t) * entries, "decoded rows");
+    alloc(m_sigCol, sizeof(uint32_t) * entries, "decoded columns");
+    alloc(m_sigVal, sizeof(double) * entries, "decoded values");
+    alloc(m_sigKeep, sizeof(int) * (entries + 1), "decoded mask");
+    check(sig_decode(m_stream, (int)chunks.size(), m_sigChunks.as<SigChunk>(), m_sigBuf.as<unsigned char>(), groups,
+                     m_sigRow.as<uint32_t>(), m_sigCol.as<uint32_t>(), m_sigVal.as<double>(), m_sigKeep.as<int>()),
+          "decode");
+    check(cudaMemsetAsync(m_sigKeep.as<int>() + entries, 0, sizeof(int), m_stream), "memset");
+    alloc(m_cscScratch, sizeof(int) * (entries + 8), "positions");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count((int)entries + 1) + 16), "scan scratch");
+    check(scan_exclusive(m_stream, m_sigKeep.as<int>(), m_cscScratch.as<int>(), (int)entries + 1, m_blockSums.as<int>()),
+          "scan");
+    int kept = 0;
+    check(cudaMemcpyAsync(&kept, m_cscScratch.as<int>() + entries, sizeof(int), cudaMemcpyDeviceToHost, m_stream),
+          "D2H");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    if (kept == 0) throw InvalidValue("partitioned matrix holds no non-zero entry.");
+    alloc(m_inRow, sizeof(uint32_t) * kept, "COO rows");
+    alloc(m_inCol, sizeof(uint32_t) * kept, "COO cols");
+    alloc(m_inVal, sizeof(double) * kept, "COO values");
+    check(sig_compact(m_stream, entries, m_cscScratch.as<int>(), m_sigKeep.as<int>(), m_sigRow.as<uint32_t>(),
+                      m_sigCol.as<uint32_t>(), m_sigVal.as<double>(), m_inRow.as<uint32_t>(), m_inCol.as<uint32_t>(),
+                      m_inVal.as<double>()),
+          "compact");
+    // The compacted list is a COO input in stored order (base 0).
+    const uint64_t nnz = (uint64_t)kept;
+    const uint64_t nnzPad = (nnz + 3) / 4 * 4 + 4;
+    alloc(m_rowptr, sizeof(int) * ((size_t)n + 1 + kRowptrPad), "CSR row pointers");
+    alloc(m_col, sizeof(int) * nnzPad, "CSR columns");
+    alloc(m_val, sizeof(double) * nnzPad, "CSR values");
+    alloc(m_perm, sizeof(uint32_t) * (nnz + 1), "CSR permutation");
+    alloc(m_counts, sizeof(int) * ((size_t)n + 2), "conversion counts");
+    alloc(m_fill, sizeof(int) * ((size_t)n + 1), "conversion fill");
+    alloc(m_keys, sizeof(uint64_t) * (nnz + 1), "conversion keys");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count((int)std::max<uint64_t>(n + 1, nnz + 1)) + 16),
+          "scan scratch");
+    ConvertScratch sc;
+    sc.counts = m_counts.as<int>();
+    sc.fill = m_fill.as<int>();
+    sc.blockSums = m_blockSums.as<int>();
+    sc.keys = m_keys.as<uint64_t>();
+    sc.flags = m_flags.as<int>();
+    int herr = 0;
+    check(coo_to_csr(m_stream, (int)n, (int64_t)nnz, m_inRow.as<uint32_t>(), m_inCol.as<uint32_t>(), 0,
+                     m_rowptr.as<int>(), m_col.as<int>(), m_perm.as<uint32_t>(), sc, &herr),
+          "COO to CSR conversion");
+    if (herr & kStatusIndexError) throw InvalidValue("decoded index out of range.");
+    check(gather_values(m_stream, (int64_t)nnz, m_perm.as<uint32_t>(), m_inVal.as<double>(), m_val.as<double>()),
+          "value gather");
+    m_n = n;
+    m_nnz = nnz;
+    m_kind = 4;
+    m_sigRows = totalRows;
+    finishMatrix();
+}
+
+void PcgHandle::signatureSpmv(const double* x, uint32_t xLen, double* y, uint32_t yRows, uint32_t startAddr,
+                              unsigned char* frame, uint64_t frameBytes) {
+    if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
+    if (xLen > m_n || yRows > m_n) throw InvalidValue("vector longer than the matrix.");
+    alloc(m_scratchY, sizeof(double) * ((size_t)m_n4 + 4), "SpMV output");
+    check(cudaMemsetAsync(m_b.p, 0, sizeof(double) * m_n4, m_stream), "memset");
+    check(cudaMemcpyAsync(m_b.p, x, sizeof(double) * xLen, cudaMemcpyHostToDevice, m_stream), "H2D x");
+    check(spmv64(m_spmvCfg, m_spmvGrid, m_b.as<double>(), m_scratchY.as<double>(), nullptr, m_state.as<CgState>(),
+                 m_partials.as<double>(), kSpmvPlain, nullptr),
+          "SpMV");
+    if (y) check(cudaMemcpyAsync(y, m_scratchY.p, sizeof(double) * yRows, cudaMemcpyDeviceToHost, m_stream), "D2H y");
+    if (frame) {
+        const uint64_t need = 64 + 64 * (uint64_t)(yRows == 0 ? 1 : (yRows + 7) / 8);
+        if (frameBytes < need) throw InvalidValue("frame buffer too small.");
+        alloc(m_sigFrame, need, "frame");
+        check(transy_frame(m_stream, startAddr, yRows, m_scratchY.as<double>(), m_sigFrame.as<unsigned char>()),
+              "frame");
+        check(cudaMemcpyAsync(frame, m_sigFrame.p, need, cudaMemcpyDeviceToHost, m_stream), "D2H frame");
+    }
+    check(cudaStreamSynchronize(m_stream), "sync");
 }
 
 // ---------------------------------------------------------------------------

@@ -84,6 +84,12 @@ class PcgHandle {
     void copyX64(double* x, uint32_t n, bool toDevice);
 
     void spmv(const double* x, double* y, bool onDevice);
+    // The reference's partitioned-matrix buffers as the stored matrix.
+    void setSignatureMatrix(uint32_t nch, const void* const* bufs, const uint64_t* bytes, const void* par,
+                            uint64_t parBytes, const void* rb, uint64_t rbBytes);
+    void signatureSpmv(const double* x, uint32_t xLen, double* y, uint32_t yRows, uint32_t startAddr,
+                       unsigned char* frame, uint64_t frameBytes);
+    uint32_t sigRows() const { return m_sigRows; }
     // Adjoint of the last solve: lambda = A^-1 g; optional dL/dA per input entry.
     Results adjoint(const double* g, const double* diag, double* lambda, double* gradA, uint32_t maxIter, double tol,
                     bool onDevice);
@@ -181,6 +187,9 @@ class PcgHandle {
     // mixed precision
     DevBuf m_state32, m_r32, m_p32, m_d32, m_Ap32, m_J32;
 
+    // signature input
+    DevBuf m_sigBuf, m_sigChunks, m_sigRow, m_sigCol, m_sigVal, m_sigKeep, m_sigFrame;
+    uint32_t m_sigRows = 0;
     // adjoint
     DevBuf m_xKeep, m_lambda, m_grad, m_edgeI, m_edgeJ, m_edgeC, m_edgeG;
     bool m_haveX = false, m_haveLambda = false;

@@ -7,7 +7,8 @@
 // consecutive steps, so every thread does the same amount of work however
 // the entries are spread over rows (a 4000-entry row costs the same as 4000
 // rows of one entry).  The CTA stages its row ends and its entries into shared
-// memory with coalesced loads, each thread finds its start by a binary search
+// memory with coalesced loads (gathering x[col] for every entry while it does,
+// so the gathers are all in flight at once), each thread finds its start by a binary search
 // on the diagonal, walks its steps, and hands the partial sum of an unfinished
 // row to its successor.  Rows that cross threads are finished in the CTA by
 // adding the carries of the preceding threads in thread order; rows that
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(kMT) spmv_merge_kernel(int n, int nnz, const i
     typedef typename MergeAcc<VT>::type AccT;
     __shared__ int sRowEnd[kTile + 1];      // rowptr[i0+1 ..] for the tile's rows
     __shared__ VT sVal[kTile];
-    __shared__ int sCol[kTile];
+    __shared__ VT sXg[kTile];  // x gathered at the entry's column while staging
     __shared__ int sCarryRow[kMT];
     __shared__ AccT sCarryVal[kMT];
     __shared__ int sBounds[4];
@@ -92,9 +93,11 @@ __global__ void __launch_bounds__(kMT) spmv_merge_kernel(int n, int nnz, const i
     // Stage row ends of rows i0 .. min(i1, n-1) and the entries j0 .. j1 - 1.
     const int nrows = min(i1, n - 1) - i0 + 1;
     for (int k = tid; k < nrows; k += kMT) sRowEnd[k] = rowptr[i0 + 1 + k];
+    // The gathers of x are issued here, all independent, instead of one per
+    // step inside the sequential walk below.
     for (int k = tid; k < j1 - j0; k += kMT) {
         sVal[k] = val[j0 + k];
-        sCol[k] = col[j0 + k];
+        sXg[k] = __ldg(&x[col[j0 + k]]);
     }
     __syncthreads();
 
@@ -121,7 +124,7 @@ __global__ void __launch_bounds__(kMT) spmv_merge_kernel(int n, int nnz, const i
     for (int d = dt; d < de; ++d) {
         const int rend = i < n ? sRowEnd[i - i0] : nnz;
         if (j < rend) {
-            acc = fma((AccT)sVal[j - j0], (AccT)__ldg(&x[sCol[j - j0]]), acc);
+            acc = fma((AccT)sVal[j - j0], (AccT)sXg[j - j0], acc);
             ++j;
         } else {
             // row i ends here

@@ -54,24 +54,21 @@ cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, d
 int vec_grid(int n4, int numSms);
 cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x,
                            double* r, double* p, double* J, double* Ap, CgState* state, double* partials);
-cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, const double* Ap, const double* J,
-                             CgState* state, double* partials);
-cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* r,
-                              const double* J, CgState* state);
+cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* x, double* r, const double* p,
+                             const double* Ap, const double* J, CgState* state, double* partials);
+cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* p, const double* r, const double* J,
+                              CgState* state);
 
-// ---- mixed precision (mixed_kernels.cu) ----
-cudaError_t ir_init_launch(int grid, cudaStream_t s, int n, int n4, const double* b, const double* diag, double* x,
-                           float* J32, CgState* st, double* partials);
-cudaError_t ir_check_launch(cudaStream_t s, CgState* st, CgState* in, uint64_t outerHandle, uint32_t maxOuter);
-cudaError_t ir_inner_init_launch(int grid, cudaStream_t s, int n4, const double* r64, const float* J32, float* r32,
-                                 float* p32, float* d32, CgState* st, CgState* in, double* partials,
-                                 uint64_t innerHandle, double innerTol);
-cudaError_t cg32_update_launch(int grid, cudaStream_t s, int n4, float* r, const float* Ap, const float* J,
-                               CgState* in, double* partials, uint64_t innerHandle, int useCond);
-cudaError_t cg32_pupdate_launch(int grid, cudaStream_t s, int n4, float* d, float* p, const float* r, const float* J,
-                                CgState* in);
-cudaError_t ir_update_launch(int grid, cudaStream_t s, int n4, double* x, const float* d, CgState* st,
-                             const CgState* in);
+// ---- mixed precision, reliable updates (mixed_kernels.cu) ----
+cudaError_t rel_init_launch(int grid, cudaStream_t s, int n, int n4, const double* b, const double* diag, double* x,
+                            float* d, float* J, float* r, float* p, CgState* st, double* partials);
+cudaError_t rel_update_launch(int grid, cudaStream_t s, int n4, float* d, float* r, const float* p, const float* Ap,
+                              const float* J, CgState* st, double* partials);
+cudaError_t rel_fold_launch(int grid, cudaStream_t s, int n4, double* x, float* d, const CgState* st);
+cudaError_t rel_restart_launch(int grid, cudaStream_t s, int n4, const double* r64, const float* J, float* r,
+                               CgState* st, double* partials);
+cudaError_t rel_pupdate_launch(int grid, cudaStream_t s, int n4, float* p, const float* r, const float* J,
+                               CgState* st);
 
 // ---- batched solves (batched_kernels.cu) ----
 struct BatchResult {      // layout of XJPCG_GbBatchResult_t
@@ -113,6 +110,19 @@ cudaError_t batch_validate_columns(cudaStream_t st, int nsys, const int* sysRow,
 void batch_config_shape(int cfg, int* threads, int* lanes);
 cudaError_t batch_launch(int cfg, bool mixed, int numSms, int smemRows, cudaStream_t st, const BatchLaunch& L,
                          int* gridOut);
+
+// ---- partitioned-matrix ("signature") input (signature_kernels.cu) ----
+struct SigChunk {
+    int64_t byteStart;   // offset of the chunk in the concatenated channel buffers
+    int64_t groupStart;  // first global 4-entry group of the chunk
+    int32_t rowBase;     // row-block start + the channel's row offset
+    int32_t colBase;     // partition base column block + the channel's offset
+};
+cudaError_t sig_decode(cudaStream_t st, int nchunks, const SigChunk* chunks, const unsigned char* buf, int64_t groups,
+                       uint32_t* row, uint32_t* col, double* val, int* keep);
+cudaError_t sig_compact(cudaStream_t st, int64_t count, const int* pos, const int* keep, const uint32_t* row,
+                        const uint32_t* col, const double* val, uint32_t* rowOut, uint32_t* colOut, double* valOut);
+cudaError_t transy_frame(cudaStream_t st, uint32_t startAddr, uint32_t rows, const double* y, unsigned char* frame);
 
 // ---- adjoint (adjoint_kernels.cu) ----
 cudaError_t grad_nnz_launch(cudaStream_t st, int n, const int* rowptr, const int* col, const uint32_t* perm,

@@ -40,9 +40,12 @@ struct alignas(16) CgState {
     IterRecord* records;           // slot 0 = command, slot k+1 = iteration k
     uint64_t condHandle;           // cudaGraphConditionalHandle of the loop
     uint32_t useCond;              // 1 when running under a conditional node
-    uint32_t outer;                // mixed precision: refinement sweeps
-    uint32_t innerK;               // mixed precision: inner iterations total
-    uint32_t xTag;                 // iteration whose x update has been applied
+    uint32_t outer;                // mixed precision: reliable updates (true-residual refreshes)
+    uint32_t innerK;               // mixed precision: FP32 iterations
+    uint32_t reliable;             // mixed precision: this iteration refreshes the residual
+    double rrMax;                  // mixed precision: largest r.r since the last refresh
+    double delta2;                 // mixed precision: refresh when r.r < delta2 * rrMax
+    uint64_t relHandle;            // mixed precision: conditional handle of the refresh
 };
 
 }  // namespace xjpcg

@@ -72,6 +72,28 @@ XJPCG_Status_t xJPCG_gbSolveDevice(XJPCG_Handle_t* handle, const double* d_b, co
 XJPCG_Status_t xJPCG_gbMixedSolve(XJPCG_Handle_t* handle, const double* b, const double* diagA, double* x,
                                   uint32_t maxIter, double tol, uint32_t* iter, double* res, int onDevice);
 
+/* SpmvHost drop-in (replaces L2/sparse/include/sw/fp64/spmvHost.hpp:26-103:
+ * createLoadNnzBufs + createLoadParXbufs[0] + createLoadRbParamBufs +
+ * sendBOs).  Takes the reference's partitioned-matrix buffers as written by
+ * its host partitioner (nnzVal_0..15, parParam, rbParam; numChannels must be
+ * 16), decodes them on the GPU and stores the matrix in the handle (padding
+ * and zero-valued entries dropped).  The matrix is square of size
+ * max(rows, padded columns); xJPCG_gbGetInfo reports it. */
+XJPCG_Status_t xJPCG_gbSetSignatureMatrix(XJPCG_Handle_t* handle, uint32_t numChannels, const void* const* nnzBufs,
+                                          const uint64_t* nnzBytes, const void* parParam, uint64_t parParamBytes,
+                                          const void* rbParam, uint64_t rbParamBytes);
+
+/* y = A x for the matrix loaded by xJPCG_gbSetSignatureMatrix (SpmvHost run +
+ * getY; the x buffer is the second createLoadParXbufs buffer).  x has xLen
+ * entries (the padded column count, zero-extended), y receives yRows rows
+ * (setStoreYrows).  When frame is not NULL it also receives the dSpmv
+ * transY framing of those rows (dSpmv/hw/include/impl/transY.hpp:35-65): a
+ * 64-byte word {startAddr, yRows, 0...} followed by the values packed eight
+ * per 64-byte word, zero-filled, at least one data word; frameBytes must be
+ * >= 64 + 64 * max(1, ceil(yRows / 8)). */
+XJPCG_Status_t xJPCG_gbSignatureSpmv(XJPCG_Handle_t* handle, const double* x, uint32_t xLen, double* y,
+                                     uint32_t yRows, uint32_t startAddr, void* frame, uint64_t frameBytes);
+
 /* Adjoint of the handle's last solve x = A^-1 b (no counterpart in the
  * reference).  With g = dL/dx, solves lambda = A^-1 g (A is SPD) with the
  * same fp64 JPCG and stop rule, then, when gradA is not NULL, writes

@@ -115,3 +115,18 @@ def stored_order(dec):
     row, part, pos = dec["row"][keep], dec["part"][keep], dec["pos"][keep]
     order = np.lexsort((pos, part, row))
     return {k: dec[k][keep][order] for k in ("row", "col", "val", "part")}
+
+
+def transy_frame(start_addr: int, rows: int, y) -> bytes:
+    """The dSpmv transY framing (dSpmv/hw/include/impl/transY.hpp:35-65) of
+    the first `rows` values of y: one 64-byte word {start_addr, rows, 0...}
+    (uint32 little endian), then the values packed eight per 64-byte word in
+    arrival order, the last word zero-filled; the HLS loop always emits a final
+    data word, so rows = 0 still yields one zero word."""
+    head = np.zeros(16, np.uint32)
+    head[0] = start_addr
+    head[1] = rows
+    words = max(1, (rows + 7) // 8)
+    data = np.zeros(words * 8, np.float64)
+    data[:rows] = np.asarray(y, np.float64)[:rows]
+    return head.tobytes() + data.tobytes()
