@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--cpu-sample-iters", type=int, default=40)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the mixed-precision, batched and adjoint measurements")
     return ap.parse_args()
 
 
@@ -150,6 +152,89 @@ def cpu_sample(sysm, iters_full, sample_iters, nthreads=0):
     dt = time.perf_counter() - t0
     per_iter = dt / sample_iters
     return per_iter, dt
+
+
+def _timed(fn, reps=3):
+    """Median wall time of fn() over reps (device work synchronised inside)."""
+    import torch
+    ts = []
+    out = None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts)), out
+
+
+def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
+    """fp64 JPCG and the reliable-update mixed solver on the same system, both
+    to 1e-10, with their errors against a tight FP64 oracle solve."""
+    import torch
+    import oracle
+    h = X.JPCG()
+    r = h.csr_solve(sysm.n, sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 0, 1e-10)
+    d_b = torch.from_numpy(sysm.b).cuda()
+    d_d = torch.from_numpy(sysm.diag).cuda()
+    d_x = torch.zeros_like(d_b)
+    _timed(lambda: h.solve_device(d_b.data_ptr(), d_d.data_ptr(), d_x.data_ptr(), 20000, 1e-10), 1)
+    t64, (st64, it64, _) = _timed(lambda: h.solve_device(d_b.data_ptr(), d_d.data_ptr(), d_x.data_ptr(), 20000,
+                                                         1e-10))
+    x64 = d_x.cpu().numpy()
+    _timed(lambda: h.mixed_solve(d_b.data_ptr(), d_d.data_ptr(), 20000, 1e-10, x=d_x.data_ptr(), on_device=True), 1)
+    tm, m = _timed(lambda: h.mixed_solve(d_b.data_ptr(), d_d.data_ptr(), 20000, 1e-10, x=d_x.data_ptr(),
+                                         on_device=True))
+    inf = h.info()
+    xm = d_x.cpu().numpy()
+    tight = oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 200000, tight_tol)["x"]
+    nt = np.linalg.norm(tight)
+    out = {"system": name, "n": sysm.n, "nnz": sysm.nnz, "fp64_time_to_tol_s": t64, "fp64_iters": it64,
+           "fp64_status": st64, "mixed_time_to_tol_s": tm, "mixed_fp32_iters": inf.innerIters,
+           "mixed_refreshes": inf.outerSweeps, "mixed_status": m.status, "speedup": t64 / tm,
+           "fp64_err_vs_oracle": float(np.linalg.norm(x64 - tight) / nt),
+           "mixed_err_vs_oracle": float(np.linalg.norm(xm - tight) / nt),
+           "mixed_true_relres": float(oracle.true_relres(sysm.rowptr, sysm.col, sysm.val, sysm.b, xm)),
+           "oracle": "oracle JPCG to %g (FP64, CPU)" % tight_tol,
+           "spmv_layout": ["csr_staged", "sliced", "merge_path"][inf.spmvLayout]}
+    h.close()
+    return out
+
+
+def batched_measure(X, count=4096):
+    from hpc_gb300 import workloads as W
+    systems = W.batched_stencils(count=count, seed=3)
+    h = X.JPCG()
+    out = {"systems": count, "rows": int(sum(s.n for s in systems)), "nnz": int(sum(s.nnz for s in systems))}
+    for prec, key in ((0, "fp64"), (1, "mixed")):
+        st, _, res = h.batch_solve(systems, 20000, 1e-10, precision=prec)  # includes tuning on first use
+        st, _, res = h.batch_solve(systems, 20000, 1e-10, precision=prec)
+        inf = h.info()
+        out[key] = {"status": st, "device_ms": inf.batchMs, "systems_per_s": count / (inf.batchMs / 1e3),
+                    "converged": int(np.sum((res["status"] == 0) & (res["res"] <= 1e-10))),
+                    "iters_total": int(res["itersRun"].sum()), "threads": inf.batchThreads,
+                    "lanes": inf.batchLanes, "smem_rows": inf.batchSmemRows, "grid": inf.batchGrid}
+    h.close()
+    return out
+
+
+def adjoint_measure(X, nx=96):
+    import torch
+    from hpc_gb300 import workloads as W
+    prob = W.adjoint_problem(nx, seed=4)
+    n = nx ** 3
+    ghost = W.ghost_diagonal7(prob.shape, prob.ghost)
+    s = W.assemble_edges(n, prob.edge_i, prob.edge_j, np.exp(prob.theta), ghost)
+    h = X.JPCG()
+    tf, r = _timed(lambda: h.csr_solve(n, s.rowptr, s.col, s.val, s.diag, prob.b, 20000, 1e-12,
+                                       mode=X.MODE_KEEP_MATRIX if h.info().n == n else X.MODE_DEFAULT), 3)
+    g = r.x - 0.5 * r.x  # any right-hand side of the right size for the timing
+    ta, (st, lam, _, it, res) = _timed(lambda: h.adjoint(g, s.diag, 20000, 1e-12), 3)
+    tg, _ = _timed(lambda: h.edge_grad(prob.edge_i, prob.edge_j, np.exp(prob.theta)), 3)
+    h.close()
+    return {"grid": "%d^3" % nx, "n": n, "edges": int(prob.edge_i.size), "forward_solve_s": tf,
+            "forward_iters": r.iters, "adjoint_solve_s": ta, "adjoint_iters": it, "edge_gradient_s": tg,
+            "tol": 1e-12, "note": "host-array calls (H2D/D2H inside); gradient checked in tests/test_gpu_adjoint.py"}
 
 
 def run_reference(args):
@@ -311,6 +396,14 @@ def run_gb300(args):
                "sample": "%d oracle JPCG iterations on the full 160^3 system (%.1f s), scaled to the %d "
                          "iterations of the GPU solve" % (S, dt, k_iters)}
 
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        from hpc_gb300 import workloads as W
+        extras["mixed"] = [mixed_vs_fp64(X, sysm, "diffusion27_160"),
+                           mixed_vs_fp64(X, W.zipf_spd(2_000_000, seed=2), "zipf_spd_2M")]
+        extras["batched"] = batched_measure(X)
+        extras["adjoint"] = adjoint_measure(X)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ttt * 1e3, "higher_is_better": True,
@@ -328,6 +421,7 @@ def run_gb300(args):
                              "traffic_source": traffic_src},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clock_info,
                 "loop": "conditional-graph" if h.info().loopMode == 1 else "host"}
+        line.update(extras)
         print(json.dumps(line), flush=True)
     h.close()
     if world > 1:

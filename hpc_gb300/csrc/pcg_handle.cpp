@@ -254,6 +254,7 @@ void PcgHandle::finishMatrix() {
     m_val32Valid = false;
     m_sellState = 0;
     m_sell32Valid = false;
+    m_mergeTilesValid = false;
     check(cudaStreamSynchronize(m_stream), "sync");
     m_haveMatrix = true;
     ensureVectors(m_n);
@@ -287,6 +288,10 @@ bool PcgHandle::isMerge(int cfg) const { return cfg == spmv_num_configs() + sell
 
 void PcgHandle::ensureMergeScratch() {
     const int nt = merge_tiles((int)m_n, (int64_t)m_nnz);
+    if (m_mergeTilesValid && (size_t)nt + 1 <= m_mergeTile.bytes / sizeof(int)) return;
+    alloc(m_mergeTile, sizeof(int) * ((size_t)nt + 2), "merge tile rows");
+    check(merge_partition(m_stream, (int)m_n, (int)m_nnz, m_rowptr.as<int>(), m_mergeTile.as<int>()), "merge tiles");
+    m_mergeTilesValid = true;
     alloc(m_mergeRow, sizeof(int) * ((size_t)nt + 1), "merge carries");
     alloc(m_mergeVal, sizeof(double) * ((size_t)nt + 1), "merge carries");
     alloc(m_mergePart, sizeof(double) * ((size_t)nt + merge_fixup_grid(nt) + 1), "merge partials");
@@ -315,7 +320,8 @@ cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, con
     if (isMerge(cfg)) {
         const int m = mode == kSpmvResidual ? kSpmvPlain : mode;
         cudaError_t e = spmv_merge_launch<double>(m_stream, (int)m_n, (int)m_nnz, m_rowptr.as<int>(), m_col.as<int>(),
-                                                  m_val.as<double>(), x, y, m_mergeRow.as<int>(), m_mergeVal.p,
+                                                  m_val.as<double>(), x, y, m_mergeTile.as<int>(),
+                                                  m_mergeRow.as<int>(), m_mergeVal.p,
                                                   m_mergePart.as<double>(), st, m, done);
         if (e != cudaSuccess || mode != kSpmvResidual) return e;
         return residual_finish_launch<double>(m_stream, (int)m_n, b, y, part, st);
@@ -331,7 +337,8 @@ cudaError_t PcgHandle::spmv32(int cfg, int grid, const float* x, float* y, const
                               double* part, int mode, const uint32_t* done) {
     if (isMerge(cfg))  // the fp32 inner loop only uses the kCgDot mode
         return spmv_merge_launch<float>(m_stream, (int)m_n, (int)m_nnz, m_rowptr.as<int>(), m_col.as<int>(),
-                                        m_val32.as<float>(), x, y, m_mergeRow.as<int>(), m_mergeVal.p,
+                                        m_val32.as<float>(), x, y, m_mergeTile.as<int>(), m_mergeRow.as<int>(),
+                                        m_mergeVal.p,
                                         m_mergePart.as<double>(), st, mode, done);
     if (!isSell(cfg))
         return spmv_launch<float>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),

@@ -169,6 +169,8 @@ class PcgHandle {
     DevBuf m_sliceOff, m_sellCol, m_sellVal, m_sellVal32;
     int m_sellState = 0;  // 0 not built, 1 built, 2 rejected (too much padding)
     DevBuf m_mergeRow, m_mergeVal, m_mergePart;  // merge-path carries and partials
+    DevBuf m_mergeTile;                          // merge-path tile start rows
+    bool m_mergeTilesValid = false;
     int64_t m_sellTotal = 0;
     bool m_sell32Valid = false;
     bool m_val32Valid = false;

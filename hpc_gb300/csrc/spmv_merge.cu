@@ -63,7 +63,7 @@ template <typename VT>
 __global__ void __launch_bounds__(kMT) spmv_merge_kernel(int n, int nnz, const int* __restrict__ rowptr,
                                                          const int* __restrict__ col, const VT* __restrict__ val,
                                                          const VT* __restrict__ x, VT* __restrict__ y,
-                                                         int* __restrict__ carryRow,
+                                                         const int* __restrict__ tileRow, int* __restrict__ carryRow,
                                                          typename MergeAcc<VT>::type* __restrict__ carryVal,
                                                          double* __restrict__ partials, CgState* state, int mode,
                                                          const uint32_t* doneFlag) {
@@ -81,8 +81,9 @@ __global__ void __launch_bounds__(kMT) spmv_merge_kernel(int n, int nnz, const i
     const int d0 = blockIdx.x * kTile;
     const int d1 = min(d0 + kTile, total);
     if (tid == 0) {
-        const int i0 = path_search(rowptr, d0, max(0, d0 - nnz), min(d0, n));
-        const int i1 = path_search(rowptr, d1, max(0, d1 - nnz), min(d1, n));
+        // tile start rows are computed once per matrix (merge_partition_kernel)
+        const int i0 = tileRow[blockIdx.x];
+        const int i1 = tileRow[blockIdx.x + 1];
         sBounds[0] = i0;
         sBounds[1] = d0 - i0;  // j0
         sBounds[2] = i1;
@@ -92,12 +93,28 @@ __global__ void __launch_bounds__(kMT) spmv_merge_kernel(int n, int nnz, const i
     const int i0 = sBounds[0], j0 = sBounds[1], i1 = sBounds[2], j1 = sBounds[3];
     // Stage row ends of rows i0 .. min(i1, n-1) and the entries j0 .. j1 - 1.
     const int nrows = min(i1, n - 1) - i0 + 1;
-    for (int k = tid; k < nrows; k += kMT) sRowEnd[k] = rowptr[i0 + 1 + k];
-    // The gathers of x are issued here, all independent, instead of one per
-    // step inside the sequential walk below.
-    for (int k = tid; k < j1 - j0; k += kMT) {
-        sVal[k] = val[j0 + k];
-        sXg[k] = __ldg(&x[col[j0 + k]]);
+    const int cnt = j1 - j0;
+    // Unrolled so each thread has all its loads in flight at once; the
+    // gathers of x are issued here, independent of each other, instead of one
+    // per step inside the sequential walk below.
+    int cidx[kItems];
+#pragma unroll
+    for (int u = 0; u < kItems; ++u) {
+        const int k = tid + u * kMT;
+        cidx[u] = k < cnt ? __ldcs(&col[j0 + k]) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kItems; ++u) {
+        const int k = tid + u * kMT;
+        if (k < cnt) {
+            sXg[k] = __ldg(&x[cidx[u]]);
+            sVal[k] = __ldcs(&val[j0 + k]);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u <= kItems; ++u) {
+        const int k = tid + u * kMT;
+        if (k < nrows) sRowEnd[k] = __ldg(&rowptr[i0 + 1 + k]);
     }
     __syncthreads();
 
@@ -234,17 +251,35 @@ __global__ void __launch_bounds__(kMT) spmv_merge_fixup_kernel(int ntiles, const
     }
 }
 
+// Start row of every tile's path segment (ntiles + 1 entries); the matrix
+// structure is fixed, so this runs once per matrix.
+__global__ void merge_partition_kernel(int n, int nnz, int ntiles, const int* __restrict__ rowptr,
+                                       int* __restrict__ tileRow) {
+    const int total = n + nnz;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += gridDim.x * blockDim.x) {
+        const int d = min(t * kTile, total);
+        tileRow[t] = path_search(rowptr, d, max(0, d - nnz), min(d, n));
+    }
+}
+
+cudaError_t merge_partition(cudaStream_t st, int n, int nnz, const int* rowptr, int* tileRow) {
+    const int ntiles = (int)(((int64_t)n + nnz + kTile - 1) / kTile);
+    const int grid = std::max(1, std::min((ntiles + 256) / 256, 152 * 8));
+    merge_partition_kernel<<<grid, 256, 0, st>>>(n, nnz, ntiles, rowptr, tileRow);
+    return cudaGetLastError();
+}
+
 int merge_tiles(int n, int64_t nnz) { return (int)((n + nnz + kTile - 1) / kTile); }
 int merge_fixup_grid(int ntiles) { return std::max(1, std::min((ntiles + kMT - 1) / kMT, 152 * 4)); }
 
 template <typename VT>
 cudaError_t spmv_merge_launch(cudaStream_t st, int n, int nnz, const int* rowptr, const int* col, const VT* val,
-                              const VT* x, VT* y, int* carryRow, void* carryVal, double* partials, CgState* state,
-                              int mode, const uint32_t* doneFlag) {
+                              const VT* x, VT* y, const int* tileRow, int* carryRow, void* carryVal, double* partials,
+                              CgState* state, int mode, const uint32_t* doneFlag) {
     if (n <= 0) return cudaSuccess;
     typedef typename MergeAcc<VT>::type AccT;
     const int ntiles = merge_tiles(n, nnz);
-    spmv_merge_kernel<VT><<<ntiles, kMT, 0, st>>>(n, nnz, rowptr, col, val, x, y, carryRow,
+    spmv_merge_kernel<VT><<<ntiles, kMT, 0, st>>>(n, nnz, rowptr, col, val, x, y, tileRow, carryRow,
                                                    static_cast<AccT*>(carryVal), partials, state, mode, doneFlag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -254,10 +289,10 @@ cudaError_t spmv_merge_launch(cudaStream_t st, int n, int nnz, const int* rowptr
 }
 
 template cudaError_t spmv_merge_launch<double>(cudaStream_t, int, int, const int*, const int*, const double*,
-                                               const double*, double*, int*, void*, double*, CgState*, int,
-                                               const uint32_t*);
+                                               const double*, double*, const int*, int*, void*, double*, CgState*,
+                                               int, const uint32_t*);
 template cudaError_t spmv_merge_launch<float>(cudaStream_t, int, int, const int*, const int*, const float*,
-                                              const float*, float*, int*, void*, double*, CgState*, int,
+                                              const float*, float*, const int*, int*, void*, double*, CgState*, int,
                                               const uint32_t*);
 
 }  // namespace xjpcg

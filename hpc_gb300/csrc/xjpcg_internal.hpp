@@ -39,14 +39,15 @@ cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const in
                              int mode, const uint32_t* doneFlag);
 
 // ---- merge-path SpMV (spmv_merge.cu) ----
-// Scratch per matrix: carryRow[ntiles] ints, carryVal[ntiles] accumulators
+// Scratch per matrix: tileRow[ntiles + 1] ints (merge_partition), carryRow[ntiles] ints, carryVal[ntiles] accumulators
 // (double for fp64, float for fp32), partials[ntiles + merge_fixup_grid(ntiles)].
 int merge_tiles(int n, int64_t nnz);
 int merge_fixup_grid(int ntiles);
+cudaError_t merge_partition(cudaStream_t st, int n, int nnz, const int* rowptr, int* tileRow);
 template <typename VT>
 cudaError_t spmv_merge_launch(cudaStream_t st, int n, int nnz, const int* rowptr, const int* col, const VT* val,
-                              const VT* x, VT* y, int* carryRow, void* carryVal, double* partials, CgState* state,
-                              int mode, const uint32_t* doneFlag);
+                              const VT* x, VT* y, const int* tileRow, int* carryRow, void* carryVal, double* partials,
+                              CgState* state, int mode, const uint32_t* doneFlag);
 template <typename VT>
 cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, double* partials, CgState* state);
 
