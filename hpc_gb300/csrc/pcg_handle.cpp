@@ -284,6 +284,8 @@ bool PcgHandle::isSell(int cfg) const {
     return cfg >= spmv_num_configs() && cfg < spmv_num_configs() + sell_num_configs();
 }
 
+bool PcgHandle::isSellNarrow(int cfg) const { return isSell(cfg) && sell_config_narrow(cfg - spmv_num_configs()); }
+
 bool PcgHandle::isMerge(int cfg) const { return cfg == spmv_num_configs() + sell_num_configs(); }
 
 void PcgHandle::ensureMergeScratch() {
@@ -303,7 +305,8 @@ int PcgHandle::spmvGrid64(int cfg) {
         return merge_tiles((int)m_n, (int64_t)m_nnz);
     }
     if (!isSell(cfg)) return spmv_grid<double>(cfg, (int)m_n, m_numSms);
-    return ensureSell() ? sell_grid<double>(cfg - spmv_num_configs(), (int)m_n, m_numSms) : 0;
+    if (!ensureSell() || (isSellNarrow(cfg) && !m_sellNarrow)) return 0;
+    return sell_grid<double>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
 }
 
 int PcgHandle::spmvGrid32(int cfg) {
@@ -312,6 +315,7 @@ int PcgHandle::spmvGrid32(int cfg) {
         return merge_tiles((int)m_n, (int64_t)m_nnz);
     }
     if (!isSell(cfg)) return spmv_grid<float>(cfg, (int)m_n, m_numSms);
+    if (isSellNarrow(cfg) && !m_sellNarrow) return 0;
     return sell_grid<float>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
 }
 
@@ -330,7 +334,8 @@ cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, con
         return spmv_launch<double>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
                                    m_val.as<double>(), x, y, b, st, part, mode, done);
     return spmv_sell_launch<double>(cfg - spmv_num_configs(), grid, m_stream, (int)m_n, m_sliceOff.as<int>(),
-                                    m_sellCol.as<int>(), m_sellVal.as<double>(), x, y, b, st, part, mode, done);
+                                    m_sellCol.as<int>(), m_sellNarrow ? m_sellCol16.as<int16_t>() : nullptr,
+                                    m_sellVal.as<double>(), x, y, b, st, part, mode, done);
 }
 
 cudaError_t PcgHandle::spmv32(int cfg, int grid, const float* x, float* y, const float* b, CgState* st,
@@ -344,7 +349,8 @@ cudaError_t PcgHandle::spmv32(int cfg, int grid, const float* x, float* y, const
         return spmv_launch<float>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
                                   m_val32.as<float>(), x, y, b, st, part, mode, done);
     return spmv_sell_launch<float>(cfg - spmv_num_configs(), grid, m_stream, (int)m_n, m_sliceOff.as<int>(),
-                                   m_sellCol.as<int>(), m_sellVal32.as<float>(), x, y, b, st, part, mode, done);
+                                   m_sellCol.as<int>(), m_sellNarrow ? m_sellCol16.as<int16_t>() : nullptr,
+                                   m_sellVal32.as<float>(), x, y, b, st, part, mode, done);
 }
 
 // Builds (once per matrix) the sliced copy used by the SELL kernels.  Returns
@@ -369,6 +375,16 @@ bool PcgHandle::ensureSell() {
     check(sell_fill<double>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
                             m_sliceOff.as<int>(), m_sellCol.as<int>(), m_sellVal.as<double>()),
           "sliced fill");
+    bool fits = false;
+    check(sell_narrow_fits(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_blockSums.as<int>(), &fits),
+          "sliced width");
+    m_sellNarrow = fits;
+    if (fits) {
+        alloc(m_sellCol16, sizeof(int16_t) * ((size_t)total + 64), "sliced column offsets");
+        check(sell_fill_narrow(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_sliceOff.as<int>(),
+                               m_sellCol16.as<int16_t>()),
+              "sliced offsets");
+    }
     m_sellTotal = total;
     m_sellState = 1;
     m_sell32Valid = false;
@@ -384,6 +400,10 @@ void PcgHandle::tuneSpmv() {
         best = forcedCfg;
     } else if (m_forcedLanes == -2) {
         best = spmv_num_configs() + sell_num_configs();
+    } else if (m_forcedLanes == -3) {
+        if (!ensureSell() || !m_sellNarrow)
+            throw InvalidValue("the sliced SpMV layout with 16-bit column offsets is not available for this matrix.");
+        best = spmv_num_configs() + 3;
     } else if (m_forcedLanes < 0) {
         if (!ensureSell()) throw InvalidValue("the sliced SpMV layout is not available for this matrix.");
         best = spmv_num_configs();
@@ -1155,11 +1175,12 @@ int PcgHandle::tuning(float* ms, int* shape, int cap) const {
             shape[4 * c + 2] = 8;
             shape[4 * c + 3] = 0;
         } else if (isSell(c)) {
-            // sliced layout: one lane per row, no CTA staging; chunk = unroll
+            // sliced layout: one lane per row, no CTA staging; chunk = unroll,
+            // last field = bits per stored column (32 absolute, 16 offset)
             shape[4 * c] = 1;
             shape[4 * c + 1] = 0;
             shape[4 * c + 2] = sell_config_unroll(c - spmv_num_configs());
-            shape[4 * c + 3] = 0;
+            shape[4 * c + 3] = isSellNarrow(c) ? 16 : 32;
         } else {
             spmv_config_shape(c, &shape[4 * c], &shape[4 * c + 1], &shape[4 * c + 2], &shape[4 * c + 3]);
         }
@@ -1174,7 +1195,7 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->nnz = m_nnz;
     info->itersRun = m_lastState.k;
     info->spmvLanes = isMerge(m_spmvCfg) ? 0u : (isSell(m_spmvCfg) ? 1u : (uint32_t)spmv_config_lanes(m_spmvCfg));
-    info->spmvLayout = isMerge(m_spmvCfg) ? 2u : (isSell(m_spmvCfg) ? 1u : 0u);
+    info->spmvLayout = isMerge(m_spmvCfg) ? 2u : (isSellNarrow(m_spmvCfg) ? 3u : (isSell(m_spmvCfg) ? 1u : 0u));
     info->spmvGrid = (uint32_t)m_spmvGrid;
     info->statusBits = m_lastState.status;
     info->outerSweeps = m_lastOuter;

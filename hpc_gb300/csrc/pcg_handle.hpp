@@ -130,6 +130,7 @@ class PcgHandle {
     void tuneSpmv();
     int numSpmvCfgs() const;
     bool isSell(int cfg) const;
+    bool isSellNarrow(int cfg) const;
     bool isMerge(int cfg) const;
     void ensureMergeScratch();
     int spmvGrid64(int cfg);
@@ -167,6 +168,8 @@ class PcgHandle {
     DevBuf m_counts, m_fill, m_blockSums, m_keys, m_flags, m_cscScratch;
     // sliced (SELL-32) copy of the matrix, built on demand by the tuner
     DevBuf m_sliceOff, m_sellCol, m_sellVal, m_sellVal32;
+    DevBuf m_sellCol16;          // int16 column offsets (when the matrix is narrow enough)
+    bool m_sellNarrow = false;
     int m_sellState = 0;  // 0 not built, 1 built, 2 rejected (too much padding)
     DevBuf m_mergeRow, m_mergeVal, m_mergePart;  // merge-path carries and partials
     DevBuf m_mergeTile;                          // merge-path tile start rows

@@ -334,6 +334,12 @@ template cudaError_t spmv_launch<float>(int, int, cudaStream_t, int, const int*,
 // autotuner picks this layout for matrices with near-uniform row lengths
 // (stencils) and the staged CSR kernels above for irregular ones.  Padding
 // entries hold value 0 and the row's own index as column.
+//
+// Narrow columns: when every stored column lies within 32767 of its row
+// (banded matrices, e.g. any 27-point grid up to 180 x 180 planes), the
+// column array is also kept as int16 offsets col - row, cutting the streamed
+// bytes per entry from 12 to 10 (fp64) and from 8 to 6 (fp32).  Rows past n
+// in the last slice read x[n - 1] with value 0.
 // ===========================================================================
 namespace xjpcg {
 
@@ -349,6 +355,36 @@ __global__ void sell_slice_len_kernel(int n, const int* __restrict__ rowptr, int
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
         if (lane == 0) sliceLen[s] = len * 32;
+    }
+}
+
+// Sets *tooWide when some stored column lies more than 32767 below or 32767
+// above its row, so the int16 offset copy cannot hold it.
+__global__ void sell_width_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                  int* __restrict__ tooWide) {
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+        const int rs = rowptr[row], re = rowptr[row + 1];
+        bool wide = false;
+        for (int j = rs; j < re; ++j) {
+            const int d = col[j] - row;
+            wide |= d > 32767 || d < -32767;
+        }
+        if (wide) atomicOr(tooWide, 1);
+    }
+}
+
+__global__ void sell_fill_narrow_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                        const int* __restrict__ sliceOff, int16_t* __restrict__ scol16) {
+    const int lane = threadIdx.x & 31;
+    const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
+    const int nslices = (n + 31) / 32;
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warpsPerGrid) {
+        const int off = sliceOff[s];
+        const int len = (sliceOff[s + 1] - off) / 32;
+        const int row = s * 32 + lane;
+        const int rs = row < n ? rowptr[row] : 0;
+        const int rl = row < n ? rowptr[row + 1] - rs : 0;
+        for (int j = 0; j < len; ++j) scol16[off + j * 32 + lane] = (int16_t)(j < rl ? col[rs + j] - row : 0);
     }
 }
 
@@ -378,9 +414,22 @@ __global__ void sell_fill_kernel(int n, const int* __restrict__ rowptr, const in
     }
 }
 
-template <typename VT, int U>
-__global__ void __launch_bounds__(kSellThreads) spmv_sell_kernel(int n, int nslices, const int* __restrict__ sliceOff,
-                                                                 const int* __restrict__ scol,
+// Streams one stored column (evict-first) and returns the absolute column.
+template <typename CT>
+__device__ __forceinline__ int sell_column(const CT* p, int base);
+template <>
+__device__ __forceinline__ int sell_column<int>(const int* p, int) {
+    return __ldcs(p);
+}
+template <>
+__device__ __forceinline__ int sell_column<int16_t>(const int16_t* p, int base) {
+    return base + (int)__ldcs(reinterpret_cast<const short*>(p));
+}
+
+// CT = int: absolute columns; CT = int16_t: offsets from the row.
+template <typename VT, int U, typename CT>
+__global__ void __launch_bounds__(kSellThreads, 6) spmv_sell_kernel(int n, int nslices, const int* __restrict__ sliceOff,
+                                                                 const CT* __restrict__ scol,
                                                                  const VT* __restrict__ sval, const VT* __restrict__ x,
                                                                  VT* __restrict__ y, const VT* __restrict__ b,
                                                                  CgState* state, double* partials, int mode,
@@ -394,8 +443,9 @@ __global__ void __launch_bounds__(kSellThreads) spmv_sell_kernel(int n, int nsli
         const int off = __ldg(&sliceOff[s]);
         const int len = (__ldg(&sliceOff[s + 1]) - off) >> 5;
         const int row = s * 32 + lane;
+        const int base = min(row, n - 1);
         const VT* vp = sval + off + lane;
-        const int* cp = scol + off + lane;
+        const CT* cp = scol + off + lane;
         AccT acc = AccT(0);
         int j = 0;
         for (; j + U <= len; j += U) {
@@ -404,7 +454,7 @@ __global__ void __launch_bounds__(kSellThreads) spmv_sell_kernel(int n, int nsli
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 v[u] = __ldcs(vp + (j + u) * 32);
-                c[u] = __ldcs(cp + (j + u) * 32);
+                c[u] = sell_column<CT>(cp + (j + u) * 32, base);
             }
             AccT xv[U];
 #pragma unroll
@@ -412,7 +462,8 @@ __global__ void __launch_bounds__(kSellThreads) spmv_sell_kernel(int n, int nsli
 #pragma unroll
             for (int u = 0; u < U; ++u) acc = fma((AccT)v[u], xv[u], acc);
         }
-        for (; j < len; ++j) acc = fma((AccT)__ldcs(vp + j * 32), (AccT)__ldg(&x[__ldcs(cp + j * 32)]), acc);
+        for (; j < len; ++j)
+            acc = fma((AccT)__ldcs(vp + j * 32), (AccT)__ldg(&x[sell_column<CT>(cp + j * 32, base)]), acc);
         if (row < n) {
             if (mode == kResidual) {
                 const AccT rv = (AccT)b[row] - acc;
@@ -441,17 +492,39 @@ __global__ void __launch_bounds__(kSellThreads) spmv_sell_kernel(int n, int nsli
 }
 
 namespace {
-template <typename VT, int U>
+template <typename VT, int U, typename CT>
 int sell_bps() {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_sell_kernel<VT, U>, kSellThreads, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_sell_kernel<VT, U, CT>, kSellThreads, 0) !=
+        cudaSuccess)
         return 0;
     return nb;
 }
+
+template <typename VT, typename CT>
+void sell_kernel_launch(int u, int grid, cudaStream_t st, int n, int nslices, const int* sliceOff, const CT* scol,
+                        const VT* sval, const VT* x, VT* y, const VT* b, CgState* state, double* partials, int mode,
+                        const uint32_t* doneFlag) {
+    if (u == 4)
+        spmv_sell_kernel<VT, 4, CT><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
+                                                                  partials, mode, doneFlag);
+    else if (u == 8)
+        spmv_sell_kernel<VT, 8, CT><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
+                                                                  partials, mode, doneFlag);
+    else
+        spmv_sell_kernel<VT, 2, CT><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
+                                                                  partials, mode, doneFlag);
+}
 }  // namespace
 
-int sell_num_configs() { return 3; }
-int sell_config_unroll(int cfg) { return cfg == 0 ? 4 : (cfg == 1 ? 8 : 2); }
+// Sliced configurations: 0-2 absolute int32 columns with unroll 4, 8, 2;
+// 3-4 int16 column offsets with unroll 4, 8.
+int sell_num_configs() { return 5; }
+int sell_config_unroll(int cfg) {
+    static const int u[5] = {4, 8, 2, 4, 8};
+    return u[cfg];
+}
+bool sell_config_narrow(int cfg) { return cfg >= 3; }
 
 cudaError_t sell_build(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val, int* sliceOff,
                        int* blockSums, int64_t* total) {
@@ -472,6 +545,29 @@ cudaError_t sell_build(cudaStream_t st, int n, const int* rowptr, const int* col
     return e;
 }
 
+cudaError_t sell_narrow_fits(cudaStream_t st, int n, const int* rowptr, const int* col, int* flag, bool* fits) {
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n + 255) / 256, 152 * 16));
+    sell_width_kernel<<<grid, 256, 0, st>>>(n, rowptr, col, flag);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int h = 1;
+    e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(st);
+    *fits = h == 0;
+    return e;
+}
+
+cudaError_t sell_fill_narrow(cudaStream_t st, int n, const int* rowptr, const int* col, const int* sliceOff,
+                             int16_t* scol16) {
+    const int nslices = (n + 31) / 32;
+    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, 152 * 64);
+    sell_fill_narrow_kernel<<<grid, 256, 0, st>>>(n, rowptr, col, sliceOff, scol16);
+    return cudaGetLastError();
+}
+
 template <typename VT>
 cudaError_t sell_fill(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val,
                       const int* sliceOff, int* scol, VT* sval) {
@@ -484,7 +580,11 @@ cudaError_t sell_fill(cudaStream_t st, int n, const int* rowptr, const int* col,
 template <typename VT>
 int sell_grid(int cfg, int n, int numSms) {
     const int u = sell_config_unroll(cfg);
-    const int bps = u == 4 ? sell_bps<VT, 4>() : (u == 8 ? sell_bps<VT, 8>() : sell_bps<VT, 2>());
+    int bps;
+    if (sell_config_narrow(cfg))
+        bps = u == 4 ? sell_bps<VT, 4, int16_t>() : sell_bps<VT, 8, int16_t>();
+    else
+        bps = u == 4 ? sell_bps<VT, 4, int>() : (u == 8 ? sell_bps<VT, 8, int>() : sell_bps<VT, 2, int>());
     if (bps <= 0) return 0;
     const int nslices = (n + 31) / 32;
     const int need = (nslices + kSellThreads / 32 - 1) / (kSellThreads / 32);
@@ -493,20 +593,19 @@ int sell_grid(int cfg, int n, int numSms) {
 
 template <typename VT>
 cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const int* sliceOff, const int* scol,
-                             const VT* sval, const VT* x, VT* y, const VT* b, CgState* state, double* partials,
-                             int mode, const uint32_t* doneFlag) {
+                             const int16_t* scol16, const VT* sval, const VT* x, VT* y, const VT* b, CgState* state,
+                             double* partials, int mode, const uint32_t* doneFlag) {
     if (n <= 0) return cudaSuccess;
     const int nslices = (n + 31) / 32;
     const int u = sell_config_unroll(cfg);
-    if (u == 4)
-        spmv_sell_kernel<VT, 4><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
-                                                              partials, mode, doneFlag);
-    else if (u == 8)
-        spmv_sell_kernel<VT, 8><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
-                                                              partials, mode, doneFlag);
-    else
-        spmv_sell_kernel<VT, 2><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
-                                                              partials, mode, doneFlag);
+    if (sell_config_narrow(cfg)) {
+        if (scol16 == nullptr) return cudaErrorInvalidValue;
+        sell_kernel_launch<VT, int16_t>(u, grid, st, n, nslices, sliceOff, scol16, sval, x, y, b, state, partials,
+                                        mode, doneFlag);
+    } else {
+        sell_kernel_launch<VT, int>(u, grid, st, n, nslices, sliceOff, scol, sval, x, y, b, state, partials, mode,
+                                    doneFlag);
+    }
     return cudaGetLastError();
 }
 
@@ -516,11 +615,11 @@ template cudaError_t sell_fill<float>(cudaStream_t, int, const int*, const int*,
                                       float*);
 template int sell_grid<double>(int, int, int);
 template int sell_grid<float>(int, int, int);
-template cudaError_t spmv_sell_launch<double>(int, int, cudaStream_t, int, const int*, const int*, const double*,
-                                              const double*, double*, const double*, CgState*, double*, int,
-                                              const uint32_t*);
-template cudaError_t spmv_sell_launch<float>(int, int, cudaStream_t, int, const int*, const int*, const float*,
-                                             const float*, float*, const float*, CgState*, double*, int,
-                                             const uint32_t*);
+template cudaError_t spmv_sell_launch<double>(int, int, cudaStream_t, int, const int*, const int*,
+                                              const int16_t*, const double*, const double*, double*, const double*,
+                                              CgState*, double*, int, const uint32_t*);
+template cudaError_t spmv_sell_launch<float>(int, int, cudaStream_t, int, const int*, const int*, const int16_t*,
+                                             const float*, const float*, float*, const float*, CgState*, double*,
+                                             int, const uint32_t*);
 
 }  // namespace xjpcg

@@ -25,18 +25,23 @@ enum : int { kSpmvPlain = 0, kSpmvCgDot = 1, kSpmvResidual = 2 };
 // ---- sliced SpMV layout (spmv_kernels.cu) ----
 int sell_num_configs();
 int sell_config_unroll(int cfg);
+bool sell_config_narrow(int cfg);  // int16 column offsets instead of int32 columns
 // sliceOff must hold nslices + 1 ints; *total = stored entries (padded).
 cudaError_t sell_build(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val, int* sliceOff,
                        int* blockSums, int64_t* total);
 template <typename VT>
 cudaError_t sell_fill(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val,
                       const int* sliceOff, int* scol, VT* sval);
+// *fits = every |col - row| <= 32767 (flag: one device int of scratch).
+cudaError_t sell_narrow_fits(cudaStream_t st, int n, const int* rowptr, const int* col, int* flag, bool* fits);
+cudaError_t sell_fill_narrow(cudaStream_t st, int n, const int* rowptr, const int* col, const int* sliceOff,
+                             int16_t* scol16);
 template <typename VT>
 int sell_grid(int cfg, int n, int numSms);
 template <typename VT>
 cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const int* sliceOff, const int* scol,
-                             const VT* sval, const VT* x, VT* y, const VT* b, CgState* state, double* partials,
-                             int mode, const uint32_t* doneFlag);
+                             const int16_t* scol16, const VT* sval, const VT* x, VT* y, const VT* b, CgState* state,
+                             double* partials, int mode, const uint32_t* doneFlag);
 
 // ---- merge-path SpMV (spmv_merge.cu) ----
 // Scratch per matrix: tileRow[ntiles + 1] ints (merge_partition), carryRow[ntiles] ints, carryVal[ntiles] accumulators

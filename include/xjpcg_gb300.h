@@ -32,7 +32,8 @@ typedef struct {
     double rrLast;         /* recursive r.r after the last iteration */
     double solveMs;        /* device time of the last solve (CUDA events) */
     uint32_t loopMode;     /* 1 = conditional-graph loop, 0 = host-driven */
-    uint32_t spmvLayout;   /* 0 = CSR staged through shared memory, 1 = sliced (SELL-32), 2 = merge path */
+    uint32_t spmvLayout;   /* 0 = CSR staged through shared memory, 1 = sliced (SELL-32), 2 = merge path,
+                              3 = sliced with int16 column offsets */
     uint32_t batchThreads; /* batched solves: CTA size chosen by the tuner */
     uint32_t batchLanes;   /* batched solves: lanes per row */
     uint32_t batchSmemRows;/* batched solves: rows of p held in shared memory */
@@ -151,7 +152,8 @@ XJPCG_Status_t xJPCG_gbGetInfo(const XJPCG_Handle_t* handle, XJPCG_GbInfo_t* inf
 /* SpMV tuner report of the stored matrix: for each kernel configuration c
  * (c < *count), ms[c] = median time of a plain SpMV (-1 if not timed) and
  * shape[4c..4c+3] = lanes per row, consumer threads per CTA, chunk entries,
- * pipeline stages.  Sliced configurations report (1, 0, unroll, 0) and the
+ * pipeline stages.  Sliced configurations report (1, 0, unroll, column bits:
+ * 32 for absolute int32 columns, 16 for int16 offsets from the row) and the
  * merge-path kernel (0, 256, steps per thread, 0).  At most cap
  * configurations are written. */
 XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, int32_t* shape, int32_t cap,
@@ -161,7 +163,9 @@ XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, in
 XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream);
 
 /* Forces the CSR SpMV lanes-per-row (1, 2, 4, 8, 16, 32); -1 forces the
- * sliced layout, -2 the merge-path kernel; 0 restores tuning. */
+ * sliced layout, -2 the merge-path kernel, -3 the sliced layout with int16
+ * column offsets (INVALID_VALUE at the next solve when some column lies more
+ * than 32767 from its row); 0 restores tuning. */
 XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes);
 
 /* y = A x and *d_dot = x.y for callers that cannot allocate device memory.

@@ -45,7 +45,7 @@ def test_diffusion27_small_csr(handle):
     _check_solve(s, r)
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32, -1, -2])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32, -1, -2, -3])
 def test_every_spmv_shape_solves(handle, lanes):
     s = W.diffusion27(12, sigma=1.5, seed=7)
     rows, cols, vals = s.coo()
@@ -55,8 +55,50 @@ def test_every_spmv_shape_solves(handle, lanes):
     if lanes > 0:
         assert handle.info().spmvLanes == lanes and handle.info().spmvLayout == 0
     else:
-        assert handle.info().spmvLayout == (1 if lanes == -1 else 2)
+        assert handle.info().spmvLayout == {-1: 1, -2: 2, -3: 3}[lanes]
     _check_solve(s, r)
+
+
+def test_narrow_sliced_columns_rejected_when_too_wide(handle):
+    # one entry 40000 columns from its row: int16 offsets cannot hold it
+    n = 50000
+    rows = np.concatenate([np.arange(n), [0, 40000]]).astype(np.uint32)
+    cols = np.concatenate([np.arange(n), [40000, 0]]).astype(np.uint32)
+    vals = np.concatenate([np.full(n, 4.0), [-1.0, -1.0]])
+    diag = np.full(n, 4.0)
+    b = np.ones(n)
+    r = handle.coo_solve(n, rows, cols, vals, diag, b, 100, 1e-10)
+    assert r.status == X.SUCCESS
+    with pytest.raises(X.XJPCGError) as e:
+        handle.set_spmv_lanes(-3)
+    assert e.value.status == X.INVALID_VALUE
+    handle.set_spmv_lanes(-1)
+    r = handle.coo_solve(n, rows, cols, vals, diag, b, 100, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    assert r.status == X.SUCCESS and handle.info().spmvLayout == 1
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 1000, 40961])
+def test_narrow_sliced_spmv_ragged(handle, n):
+    # ragged last slice (rows past n read x[n-1] with value 0), random band
+    rng = np.random.default_rng(n)
+    k = 5 * n
+    rows = rng.integers(0, n, k)
+    cols = np.clip(rows + rng.integers(-min(n, 30000), min(n, 30000) + 1, k), 0, n - 1)
+    rows = np.concatenate([np.arange(n), rows]).astype(np.uint32)
+    cols = np.concatenate([np.arange(n), cols]).astype(np.uint32)
+    vals = rng.standard_normal(rows.size)
+    handle.coo_solve(n, rows, cols, vals, np.ones(n), np.ones(n), 1, 1e-10)
+    rp, cc, vv, _ = handle.get_csr()
+    x = rng.standard_normal(n)
+    handle.set_spmv_lanes(-1)
+    y32 = handle.spmv(x)
+    handle.set_spmv_lanes(-3)
+    y16 = handle.spmv(x)
+    assert handle.info().spmvLayout == 3
+    assert np.array_equal(y16, y32)  # same entries, same order
+    yref = oracle.spmv(rp, cc, vv, x)
+    scale = oracle.spmv(rp, cc, np.abs(vv), np.abs(x))
+    assert np.all(np.abs(y16 - yref) <= 1e-13 * scale)
 
 
 def test_conversion_bitexact_unsorted_fortran(handle):
