@@ -50,6 +50,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the mixed-precision, batched and adjoint measurements")
+    ap.add_argument("--profile", choices=["spmv", "solve"], default=None,
+                    help="profiling driver for ncu: set the matrix, then run --reps plain SpMVs "
+                         "(spmv) or one resident solve (solve); no timing line")
+    ap.add_argument("--workload", choices=["diffusion27", "zipf"], default="diffusion27",
+                    help="matrix of --profile: diffusion27(--nx) or the 2M-row Zipf SPD system")
+    ap.add_argument("--reps", type=int, default=4)
     return ap.parse_args()
 
 
@@ -120,26 +126,63 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per SpMV launch from the committed ncu summary (or None)."""
+def committed_traffic(layout):
+    """DRAM bytes per SpMV launch of `layout` from the committed ncu summary
+    (or None when no capture of that kernel is committed)."""
     p = os.path.join(ROOT, "profiles", "spmv_diffusion27_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
-            d = json.load(f)
-        return d.get("dram_bytes_per_launch_full"), d.get("source", p)
+            d = json.load(f).get(layout)
+        if d:
+            return d.get("dram_bytes_per_launch_full"), d.get("source", p)
     return None, None
 
 
-def spmv_bytes(n, nnz):
-    # 12 B per stored entry (f64 value + int32 column), row pointers, x read
+def run_profile(args):
+    """Profiling driver: the matrix is set through xJPCG_cooSolver (maxIter 0),
+    then --reps plain SpMVs (xJPCG_gbSpmv on device vectors) or one resident
+    solve (xJPCG_gbSolveDevice).  XJPCG_SPMV_LANES forces a layout and skips
+    the tuner's launches."""
+    import torch
+    import hpc_gb300 as X
+    from hpc_gb300 import workloads as W
+    sysm = W.diffusion27(args.nx) if args.workload == "diffusion27" else W.zipf_spd(2_000_000, seed=2)
+    rows, cols, vals = sysm.coo()
+    h = X.JPCG()
+    r = h.coo_solve(sysm.n, rows, cols, vals, sysm.diag, sysm.b, 0, 1e-10)
+    inf = h.info()
+    print("matrix n=%d nnz=%d layout=%s status=%d" % (sysm.n, sysm.nnz, LAYOUTS[inf.spmvLayout][0], r.status),
+          flush=True)
+    d_b = torch.from_numpy(sysm.b).cuda()
+    d_y = torch.zeros_like(d_b)
+    if args.profile == "spmv":
+        for _ in range(args.reps):
+            h.spmv(d_b.data_ptr(), d_y.data_ptr(), on_device=True)
+    else:
+        d_diag = torch.from_numpy(sysm.diag).cuda()
+        st, it, res = h.solve_device(d_b.data_ptr(), d_diag.data_ptr(), d_y.data_ptr(), 20000, 1e-10)
+        print("solve status=%d iters=%d res=%.3e" % (st, it, res), flush=True)
+    torch.cuda.synchronize()
+    h.close()
+
+
+# SpMV layouts as reported by xJPCG_gbGetInfo().spmvLayout
+LAYOUTS = {0: ("csr_staged", "spmv_ws_kernel (TMA-staged CSR fp64 SpMV)", 4),
+           1: ("sliced", "spmv_sell_kernel<double,U,int> (SELL-32 fp64 SpMV, int32 columns)", 4),
+           2: ("merge_path", "spmv_merge_kernel (merge-path CSR fp64 SpMV)", 4),
+           3: ("sliced16", "spmv_sell_kernel<double,U,int16_t> (SELL-32 fp64 SpMV, int16 column offsets)", 2)}
+
+
+def spmv_bytes(n, nnz, col_bytes=4):
+    # 8 B value + the stored column width per entry, row pointers, x read
     # once, y written once.
-    return 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
+    return (8 + col_bytes) * nnz + 4 * (n + 1) + 8 * n + 8 * n
 
 
-def iter_bytes(n, nnz):
+def iter_bytes(n, nnz, col_bytes=4):
     # SpMV + 11 vector streams of 8 B (update: x, p, r, Ap, J read, x, r
     # written; p kernel: r, J, p read, p written).
-    return spmv_bytes(n, nnz) + 88 * n
+    return spmv_bytes(n, nnz, col_bytes) + 88 * n
 
 
 def cpu_sample(sysm, iters_full, sample_iters, nthreads=0):
@@ -196,7 +239,7 @@ def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
            "mixed_err_vs_oracle": float(np.linalg.norm(xm - tight) / nt),
            "mixed_true_relres": float(oracle.true_relres(sysm.rowptr, sysm.col, sysm.val, sysm.b, xm)),
            "oracle": "oracle JPCG to %g (FP64, CPU)" % tight_tol,
-           "spmv_layout": ["csr_staged", "sliced", "merge_path"][inf.spmvLayout]}
+           "spmv_layout": LAYOUTS[inf.spmvLayout][0]}
     h.close()
     return out
 
@@ -365,11 +408,12 @@ def run_gb300(args):
     torch.cuda.synchronize()
     spmv_ms = e0.elapsed_time(e1) / reps
     peak, peak_kind = measured_peak()
-    B = spmv_bytes(n, nnz)
+    layout, kernel_name, col_bytes = LAYOUTS[info.spmvLayout]
+    B = spmv_bytes(n, nnz, col_bytes)
     achieved = B / (spmv_ms / 1e3) / 1e9
-    traffic, traffic_src = committed_traffic()
+    traffic, traffic_src = committed_traffic(layout)
     iter_ms = ttt * 1e3 / max(k_iters, 1)
-    iter_gbs = iter_bytes(n, nnz) / (iter_ms / 1e3) / 1e9
+    iter_gbs = iter_bytes(n, nnz, col_bytes) / (iter_ms / 1e3) / 1e9
 
     # End to end through the reference-facing COO call with host buffers.
     e2e = None
@@ -414,9 +458,9 @@ def run_gb300(args):
                 "time_to_tol_s": ttt, "iters": k_iters, "iter_ms": iter_ms, "iter_gbs": iter_gbs,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
-                             "kernel": ("spmv_sell_kernel (sliced SELL-32 fp64 SpMV)" if info.spmvLayout == 1
-                                        else "spmv_ws_kernel (TMA-staged CSR fp64 SpMV)"),
-                             "bytes_per_launch": B, "launch_ms": spmv_ms,
+                             "kernel": kernel_name, "layout": layout,
+                             "bytes_per_launch": B, "bytes_formula": "(8 + %d) nnz + 4 (n + 1) + 16 n" % col_bytes,
+                             "launch_ms": spmv_ms,
                              "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                              "traffic_source": traffic_src},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clock_info,
@@ -430,7 +474,9 @@ def run_gb300(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

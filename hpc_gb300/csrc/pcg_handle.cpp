@@ -1169,10 +1169,10 @@ int PcgHandle::tuning(float* ms, int* shape, int cap) const {
     for (int c = 0; c < ncfg && c < cap; ++c) {
         ms[c] = c < (int)m_tuneMs.size() ? m_tuneMs[c] : -1.f;
         if (isMerge(c)) {
-            // merge path: lanes 0, 256 threads, 8 path steps per thread
+            // merge path: lanes 0, 256 threads, path steps per thread
             shape[4 * c] = 0;
             shape[4 * c + 1] = 256;
-            shape[4 * c + 2] = 8;
+            shape[4 * c + 2] = merge_items_per_thread();
             shape[4 * c + 3] = 0;
         } else if (isSell(c)) {
             // sliced layout: one lane per row, no CTA staging; chunk = unroll,

@@ -32,7 +32,10 @@ namespace xjpcg {
 
 namespace {
 constexpr int kMT = 256;     // threads per CTA
-constexpr int kItems = 8;    // merge-path steps per thread
+// Merge-path steps per thread.  Odd, so that the per-thread runs of staged
+// values (read at stride ~kItems by consecutive threads) spread over the
+// shared-memory banks instead of piling onto two of them.
+constexpr int kItems = 7;
 constexpr int kTile = kMT * kItems;
 
 // Largest i in [lo, hi] with rowEnd(i-1) + i <= diag, i.e. the number of rows
@@ -270,6 +273,7 @@ cudaError_t merge_partition(cudaStream_t st, int n, int nnz, const int* rowptr, 
 }
 
 int merge_tiles(int n, int64_t nnz) { return (int)((n + nnz + kTile - 1) / kTile); }
+int merge_items_per_thread() { return kItems; }
 int merge_fixup_grid(int ntiles) { return std::max(1, std::min((ntiles + kMT - 1) / kMT, 152 * 4)); }
 
 template <typename VT>

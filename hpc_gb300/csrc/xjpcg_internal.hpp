@@ -47,6 +47,7 @@ cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const in
 // Scratch per matrix: tileRow[ntiles + 1] ints (merge_partition), carryRow[ntiles] ints, carryVal[ntiles] accumulators
 // (double for fp64, float for fp32), partials[ntiles + merge_fixup_grid(ntiles)].
 int merge_tiles(int n, int64_t nnz);
+int merge_items_per_thread();
 int merge_fixup_grid(int ntiles);
 cudaError_t merge_partition(cudaStream_t st, int n, int nnz, const int* rowptr, int* tileRow);
 template <typename VT>

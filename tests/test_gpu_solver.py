@@ -79,11 +79,13 @@ def test_narrow_sliced_columns_rejected_when_too_wide(handle):
 
 @pytest.mark.parametrize("n", [1, 31, 33, 1000, 40961])
 def test_narrow_sliced_spmv_ragged(handle, n):
-    # ragged last slice (rows past n read x[n-1] with value 0), random band
+    # ragged last slice (rows past n read x[n-1] with value 0); every row holds
+    # its diagonal and 5 random entries within 30000 columns, so slices are
+    # nearly uniform (the sliced layout rejects heavy padding)
     rng = np.random.default_rng(n)
-    k = 5 * n
-    rows = rng.integers(0, n, k)
-    cols = np.clip(rows + rng.integers(-min(n, 30000), min(n, 30000) + 1, k), 0, n - 1)
+    w = min(n - 1, 30000)
+    rows = np.repeat(np.arange(n), 5)
+    cols = np.clip(rows + rng.integers(-w, w + 1, rows.size), 0, n - 1)
     rows = np.concatenate([np.arange(n), rows]).astype(np.uint32)
     cols = np.concatenate([np.arange(n), cols]).astype(np.uint32)
     vals = rng.standard_normal(rows.size)
