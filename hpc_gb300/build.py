@@ -20,6 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libXilinxPcg.so")
 LIB_ALIAS = os.path.join(HERE, "libXilinxPcgStatic.so")
+LOADER = os.path.join(HERE, "libXilinxPcg_loader.a")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -62,9 +63,28 @@ def build_library(verbose: bool = False) -> str:
     if os.path.lexists(LIB_ALIAS):
         os.remove(LIB_ALIAS)
     os.symlink(os.path.basename(LIB), LIB_ALIAS)
+    build_loader()
     if verbose:
         print(LIB)
     return LIB
+
+
+def build_loader() -> str:
+    """libXilinxPcg_loader.a: the dlopen front end (csrc/pcg_loader.c) that an
+    application links with -ldl instead of linking libXilinxPcg.so."""
+    src = os.path.join(CSRC, "pcg_loader.c")
+    obj = os.path.join(BUILD, "pcg_loader.o")
+    deps = [src, os.path.join(ROOT, "include", "pcg.h")]
+    if os.path.exists(LOADER) and os.path.getmtime(LOADER) >= _newest(deps):
+        return LOADER
+    cc = os.environ.get("CC", "gcc")
+    for cmd in ([cc, "-std=c99", "-O2", "-fPIC", "-Wall", "-I" + os.path.join(ROOT, "include"), "-c", src, "-o", obj],
+                ["ar", "rcs", LOADER + ".tmp", obj]):
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("loader build failed (%s):\n%s\n%s" % (cmd[0], res.stdout, res.stderr))
+    os.replace(LOADER + ".tmp", LOADER)
+    return LOADER
 
 
 if __name__ == "__main__":

@@ -366,7 +366,14 @@ bool PcgHandle::ensureSell() {
     check(sell_build(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(), m_sliceOff.as<int>(),
                      m_blockSums.as<int>(), &total),
           "sliced layout");
-    if ((uint64_t)total > m_nnz + m_nnz / 2 + 64 || total > 0x7fffff00ll) {
+    // Padding of the phantom rows past n in the last slice is a fixed cost
+    // and does not count against the layout.
+    int lastOff = 0;
+    check(cudaMemcpyAsync(&lastOff, m_sliceOff.as<int>() + nslices - 1, sizeof(int), cudaMemcpyDeviceToHost, m_stream),
+          "D2H");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    const int64_t phantom = (int64_t)(nslices * 32 - (int64_t)m_n) * ((total - lastOff) / 32);
+    if ((uint64_t)(total - phantom) > m_nnz + m_nnz / 2 + 64 || total > 0x7fffff00ll) {
         m_sellState = 2;
         return false;
     }
@@ -403,7 +410,7 @@ void PcgHandle::tuneSpmv() {
     } else if (m_forcedLanes == -3) {
         if (!ensureSell() || !m_sellNarrow)
             throw InvalidValue("the sliced SpMV layout with 16-bit column offsets is not available for this matrix.");
-        best = spmv_num_configs() + 3;
+        best = spmv_num_configs() + 4;  // int16 offsets, unroll 8
     } else if (m_forcedLanes < 0) {
         if (!ensureSell()) throw InvalidValue("the sliced SpMV layout is not available for this matrix.");
         best = spmv_num_configs();
