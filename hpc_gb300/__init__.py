@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes",
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
     "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv",
+    "xJPCG_gbExportSignature", "xJPCG_gbGetSignature",
 ]
 
 
@@ -55,6 +56,12 @@ class GbInfo(C.Structure):
                 ("rrLast", C.c_double), ("solveMs", C.c_double), ("loopMode", C.c_uint32),
                 ("spmvLayout", C.c_uint32), ("batchThreads", C.c_uint32), ("batchLanes", C.c_uint32),
                 ("batchSmemRows", C.c_uint32), ("batchGrid", C.c_uint32), ("batchMs", C.c_double)]
+
+
+class GbSignature(C.Structure):
+    """XJPCG_GbSignature_t (xjpcg_gb300.h)."""
+    _fields_ = [("info", C.c_uint32 * 6), ("rowBlocks", C.c_uint32), ("partitions", C.c_uint32),
+                ("rbParamBytes", C.c_uint64), ("parParamBytes", C.c_uint64), ("nnzValBytes", C.c_uint64 * 16)]
 
 
 BATCH_RESULT_DTYPE = np.dtype([("iters", "<u4"), ("itersRun", "<u4"), ("outer", "<u4"), ("status", "<u4"),
@@ -116,6 +123,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbEdgeGrad.argtypes = [_P, i64, _P, _P, _P, _P, C.c_int]
     lib.xJPCG_gbSetSignatureMatrix.argtypes = [_P, u32, _P, _P, _P, u64, _P, u64]
     lib.xJPCG_gbSignatureSpmv.argtypes = [_P, _P, u32, _P, u32, u32, _P, u64]
+    lib.xJPCG_gbExportSignature.argtypes = [_P, _P]
+    lib.xJPCG_gbGetSignature.argtypes = [_P, _P, _P, _P]
     lib.xJPCG_gbBatchSolve.argtypes = [_P, u32, _P, _P, _P, _P, _P, _P, _P, u32, dbl, C.c_int, _P, C.c_int]
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
@@ -348,6 +357,38 @@ class JPCG:
         if st != SUCCESS:
             raise XJPCGError(st, self.last_message())
         return (y, fr) if frame else y
+
+    def export_signature(self) -> dict:
+        """The stored matrix in the reference's partitioned format:
+        {"rbParam", "parParam", "nnzVal_0".."nnzVal_15", "info"} -> bytes, the
+        contents of the files storeMatPar writes (xJPCG_gbExportSignature)."""
+        sig = GbSignature()
+        st = self.lib.xJPCG_gbExportSignature(self.h, C.byref(sig))
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        rb = np.zeros(sig.rbParamBytes, np.uint8)
+        par = np.zeros(sig.parParamBytes, np.uint8)
+        chans = [np.zeros(sig.nnzValBytes[c], np.uint8) for c in range(16)]
+        ptrs = (C.c_void_p * 16)(*[c.ctypes.data for c in chans])
+        st = self.lib.xJPCG_gbGetSignature(self.h, _ptr(rb), _ptr(par), ptrs)
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        out = {"rbParam": rb.tobytes(), "parParam": par.tobytes(),
+               "info": np.array(list(sig.info), np.uint32).tobytes()}
+        for c in range(16):
+            out["nnzVal_%d" % c] = chans[c].tobytes()
+        return out
+
+    def store_signature(self, path: str) -> dict:
+        """Writes rbParam.dat, parParam.dat, nnzVal_<c>.dat and info.dat into
+        the directory `path` (storeMatPar, gen_signature.cpp:58-81)."""
+        import os
+        files = self.export_signature()
+        os.makedirs(path, exist_ok=True)
+        for name, data in files.items():
+            with open(os.path.join(path, name + ".dat"), "wb") as f:
+                f.write(data)
+        return files
 
     def spmv_tuning(self):
         """[(lanes, consumers, chunk, stages, ms)] of the last SpMV tuning."""

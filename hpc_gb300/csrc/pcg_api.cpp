@@ -326,6 +326,18 @@ XJPCG_Status_t xJPCG_gbSignatureSpmv(XJPCG_Handle_t* handle, const double* x, ui
     XJ_GUARD_END("SpMV returns successfully")
 }
 
+XJPCG_Status_t xJPCG_gbExportSignature(XJPCG_Handle_t* handle, XJPCG_GbSignature_t* sig) {
+    XJ_GUARD_BEGIN
+    p->exportSignature(sig);
+    XJ_GUARD_END("signature exported successfully")
+}
+
+XJPCG_Status_t xJPCG_gbGetSignature(XJPCG_Handle_t* handle, void* rbParam, void* parParam, void* const* nnzVal) {
+    XJ_GUARD_BEGIN
+    p->getSignature(rbParam, parParam, nnzVal);
+    XJ_GUARD_END("signature copied successfully")
+}
+
 XJPCG_Status_t xJPCG_gbAdjointSolve(XJPCG_Handle_t* handle, const double* g, const double* diagA, double* lambda,
                                     double* gradA, uint32_t maxIter, double tol, uint32_t* iter, double* res,
                                     int onDevice) {

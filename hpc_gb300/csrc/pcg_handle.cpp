@@ -255,6 +255,7 @@ void PcgHandle::finishMatrix() {
     m_sellState = 0;
     m_sell32Valid = false;
     m_mergeTilesValid = false;
+    ++m_structGen;
     check(cudaStreamSynchronize(m_stream), "sync");
     m_haveMatrix = true;
     ensureVectors(m_n);
@@ -1160,6 +1161,30 @@ void PcgHandle::getCsr(int32_t* rowPtr, int32_t* colIdx, double* values, uint32_
         check(cudaMemcpyAsync(values, m_val.p, sizeof(double) * m_nnz, cudaMemcpyDeviceToHost, m_stream), "D2H");
     if (perm) check(cudaMemcpyAsync(perm, m_perm.p, sizeof(uint32_t) * m_nnz, cudaMemcpyDeviceToHost, m_stream), "D2H");
     check(cudaStreamSynchronize(m_stream), "sync");
+}
+
+void PcgHandle::exportSignature(XJPCG_GbSignature_t* sig) {
+    if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
+    if (!m_sigExport.valid || m_sigExport.structGen != m_structGen) {
+        m_sigExport.build(m_stream, m_n, m_nnz, m_rowptr.as<int>(), m_col.as<int>());
+        m_sigExport.structGen = m_structGen;
+    }
+    m_sigExport.format(m_stream, m_val.as<double>());
+    if (sig) {
+        std::memset(sig, 0, sizeof(*sig));
+        const SigExport& e = m_sigExport;
+        const uint32_t info[6] = {e.m, e.n, e.nnz, e.m, (e.n + 3) / 4 * 4, e.nnzPad};
+        std::memcpy(sig->info, info, sizeof(info));
+        sig->rowBlocks = (uint32_t)e.nb;
+        sig->partitions = (uint32_t)e.P;
+        sig->rbParamBytes = e.rbBytes;
+        sig->parParamBytes = e.parBytes;
+        for (int c = 0; c < 16; ++c) sig->nnzValBytes[c] = e.chanBytes[c];
+    }
+}
+
+void PcgHandle::getSignature(void* rb, void* par, void* const* nnzVal) {
+    m_sigExport.copyOut(m_stream, rb, par, nnzVal);
 }
 
 uint64_t PcgHandle::getRecords(void* buf, uint64_t cap) {

@@ -59,6 +59,33 @@ struct Results {
     uint32_t status;
 };
 
+// The stored matrix in the reference's partitioned ("signature") format,
+// built on the device (signature_export.cu).  build() computes the layout
+// from the CSR structure; format() writes the channel streams from the
+// values, so a values-only update reruns format() alone.
+class SigExport {
+   public:
+    void build(cudaStream_t st, uint32_t n, uint64_t nnz, const int* rowptr, const int* col);
+    void format(cudaStream_t st, const double* val);
+    void copyOut(cudaStream_t st, void* rb, void* par, void* const* nnzVal) const;
+
+    bool valid = false;
+    uint64_t structGen = 0;  // matrix structure the layout was built for
+    uint32_t m = 0, n = 0, nnz = 0, nnzPad = 0;
+    int nb = 0, P = 0, S = 0;
+    uint64_t rbBytes = 0, parBytes = 0;
+    uint64_t chanBytes[16] = {}, chanBase[16] = {};
+
+   private:
+    static void grow(DevBuf& b, size_t bytes, const char* what);
+    DevBuf bBlkRow0, bBlkEnt, bBlkM, bBlkMin, bBlkMax, bBlkMinG, bBlkMaxG, bBlkNcol, bBitOff, bSlotOff, bBitmap;
+    DevBuf bStarts, bNPart, bParBase, bPartG0, bPartBlock, bBlockSums;
+    DevBuf bSegCount, bSegBase, bSegLo, bSegHi, bSegRow, bSegLen, bSegMinG, bSegMaxG, bSegOff, bTotal, bPpad;
+    DevBuf bSlotSrc, bGrpRow, bGrpG;
+    DevBuf bChStart, bChLen, bChMinG, bChEndRow, bChBytes, bChOff, bChanBytes, bChanBase, bChanHdr;
+    DevBuf bRb, bPar, bOut;
+};
+
 class PcgHandle {
    public:
     PcgHandle() = default;
@@ -101,6 +128,8 @@ class PcgHandle {
                         const double* values, const double* diag, const double* b, double* x, uint32_t maxIter,
                         double tol, int precision, BatchResult* results, bool onDevice);
     void getCsr(int32_t* rowPtr, int32_t* colIdx, double* values, uint32_t* perm);
+    void exportSignature(XJPCG_GbSignature_t* sig);
+    void getSignature(void* rb, void* par, void* const* nnzVal);
     uint64_t getRecords(void* buf, uint64_t cap);
     void fillInfo(XJPCG_GbInfo_t* info) const;
     int tuning(float* ms, int* shape, int cap) const;
@@ -195,6 +224,8 @@ class PcgHandle {
     // signature input
     DevBuf m_sigBuf, m_sigChunks, m_sigRow, m_sigCol, m_sigVal, m_sigKeep, m_sigFrame;
     uint32_t m_sigRows = 0;
+    SigExport m_sigExport;
+    uint64_t m_structGen = 0;  // bumped whenever a new matrix structure is stored
     // adjoint
     DevBuf m_xKeep, m_lambda, m_grad, m_edgeI, m_edgeJ, m_edgeC, m_edgeG;
     bool m_haveX = false, m_haveLambda = false;

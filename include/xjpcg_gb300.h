@@ -84,6 +84,35 @@ XJPCG_Status_t xJPCG_gbSetSignatureMatrix(XJPCG_Handle_t* handle, uint32_t numCh
                                           const uint64_t* nnzBytes, const void* parParam, uint64_t parParamBytes,
                                           const void* rbParam, uint64_t rbParamBytes);
 
+/* Sizes of the partitioned-matrix ("signature") files of the stored matrix:
+ * info[6] = m, n, nnz, mPad, nPad, nnzPad (the words of info.dat). */
+typedef struct {
+    uint32_t info[6];
+    uint32_t rowBlocks;    /* rbParam records */
+    uint32_t partitions;   /* parParam records */
+    uint64_t rbParamBytes;
+    uint64_t parParamBytes;
+    uint64_t nnzValBytes[16];
+} XJPCG_GbSignature_t;
+
+/* Signature exporter (replaces SpmPar::partitionCooMat / partitionCscSymMat /
+ * updateMat + storeMatPar: L2/sparse/include/sw/fp64/gen_signature.hpp:41-73,
+ * signature.hpp:471-561, gen_signature.cpp:58-81).  Partitions the stored
+ * matrix on the GPU into the bytes the reference's host partitioner writes
+ * for the same input: rbParam.dat, parParam.dat, nnzVal_0..15.dat and
+ * info.dat, with parEntries 4, accLatency 8, 16 channels and 4096 x 4096
+ * partitions.  The layout is kept until the matrix structure changes; after
+ * a values-only update (XJPCG_MODE_KEEP_NZ_LAYOUT) only the value streams
+ * are rewritten, as update_sig does.  Fills *sig with the buffer sizes.
+ * INVALID_VALUE when no matrix is stored or the padded matrix would exceed
+ * 2^31 entries. */
+XJPCG_Status_t xJPCG_gbExportSignature(XJPCG_Handle_t* handle, XJPCG_GbSignature_t* sig);
+
+/* Copies the buffers of the last xJPCG_gbExportSignature to host memory of
+ * the sizes it reported; any pointer, and any of the 16 nnzVal pointers, may
+ * be NULL. */
+XJPCG_Status_t xJPCG_gbGetSignature(XJPCG_Handle_t* handle, void* rbParam, void* parParam, void* const* nnzVal);
+
 /* y = A x for the matrix loaded by xJPCG_gbSetSignatureMatrix (SpmvHost run +
  * getY; the x buffer is the second createLoadParXbufs buffer).  x has xLen
  * entries (the padded column count, zero-extended), y receives yRows rows
