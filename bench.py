@@ -239,7 +239,9 @@ def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
            "mixed_err_vs_oracle": float(np.linalg.norm(xm - tight) / nt),
            "mixed_true_relres": float(oracle.true_relres(sysm.rowptr, sysm.col, sysm.val, sysm.b, xm)),
            "oracle": "oracle JPCG to %g (FP64, CPU)" % tight_tol,
-           "spmv_layout": LAYOUTS[inf.spmvLayout][0]}
+           "spmv_layout": LAYOUTS[inf.spmvLayout][0], "spmv_layout_fp32": LAYOUTS[inf.spmvLayout32][0],
+           "spmv_fp32_ms": (h.spmv_tuning32()[inf.spmvCfg32] if inf.spmvCfg32 < 64 else None),
+           "spmv_fp64_ms": h.spmv_tuning()[inf.spmvCfg][4]}
     h.close()
     return out
 

@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes",
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
     "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv",
-    "xJPCG_gbExportSignature", "xJPCG_gbGetSignature",
+    "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32",
 ]
 
 
@@ -55,7 +55,9 @@ class GbInfo(C.Structure):
                 ("outerSweeps", C.c_uint32), ("innerIters", C.c_uint32), ("bb", C.c_double),
                 ("rrLast", C.c_double), ("solveMs", C.c_double), ("loopMode", C.c_uint32),
                 ("spmvLayout", C.c_uint32), ("batchThreads", C.c_uint32), ("batchLanes", C.c_uint32),
-                ("batchSmemRows", C.c_uint32), ("batchGrid", C.c_uint32), ("batchMs", C.c_double)]
+                ("batchSmemRows", C.c_uint32), ("batchGrid", C.c_uint32), ("batchMs", C.c_double),
+                ("spmvCfg", C.c_uint32), ("spmvCfg32", C.c_uint32), ("spmvLayout32", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class GbSignature(C.Structure):
@@ -118,6 +120,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbGetStream.argtypes = [_P, C.POINTER(_P)]
     lib.xJPCG_gbSetSpmvLanes.argtypes = [_P, C.c_int]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
+    lib.xJPCG_gbGetSpmvTuning32.argtypes = [_P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
     lib.xJPCG_gbAdjointSolve.argtypes = [_P, _P, _P, _P, _P, u32, dbl, C.POINTER(u32), C.POINTER(dbl), C.c_int]
     lib.xJPCG_gbEdgeGrad.argtypes = [_P, i64, _P, _P, _P, _P, C.c_int]
@@ -397,6 +400,13 @@ class JPCG:
         cnt = C.c_int32(0)
         self.lib.xJPCG_gbGetSpmvTuning(self.h, _ptr(ms), _ptr(shape), 64, C.byref(cnt))
         return [tuple(int(v) for v in shape[4 * i:4 * i + 4]) + (float(ms[i]),) for i in range(cnt.value)]
+
+    def spmv_tuning32(self):
+        """[ms] of the mixed solver's FP32 SpMV tuning (-1: not timed)."""
+        ms = np.zeros(64, np.float32)
+        cnt = C.c_int32(0)
+        self.lib.xJPCG_gbGetSpmvTuning32(self.h, _ptr(ms), 64, C.byref(cnt))
+        return [float(v) for v in ms[:cnt.value]]
 
     def set_spmv_lanes(self, lanes: int):
         st = self.lib.xJPCG_gbSetSpmvLanes(self.h, lanes)

@@ -416,6 +416,13 @@ XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, in
     return XJPCG_STATUS_SUCCESS;
 }
 
+XJPCG_Status_t xJPCG_gbGetSpmvTuning32(const XJPCG_Handle_t* handle, float* ms, int32_t cap, int32_t* count) {
+    if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    if (ms == nullptr || count == nullptr) return XJPCG_STATUS_INVALID_VALUE;
+    *count = impl(handle)->tuning32(ms, cap);
+    return XJPCG_STATUS_SUCCESS;
+}
+
 XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream) {
     if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
     if (stream == nullptr) return XJPCG_STATUS_INVALID_VALUE;

@@ -446,7 +446,76 @@ void PcgHandle::tuneSpmv() {
     }
     m_spmvCfg = best;
     m_spmvGrid = spmvGrid64(best);
+    m_spmvCfg32 = -1;  // retuned (or follows a forced choice) at the next mixed solve
     ++m_generation;  // graphs embed the configuration
+}
+
+// FP32 values of the layout `cfg` uses (CSR copy for the staged and
+// merge-path kernels, sliced copy for the SELL kernels).
+void PcgHandle::ensureValues32(int cfg) {
+    const uint64_t nnzPad = (m_nnz + 3) / 4 * 4 + 4;
+    if (!m_val32Valid) {
+        alloc(m_val32, sizeof(float) * nnzPad, "fp32 values");
+        check(convert_f64_to_f32(m_stream, (int64_t)nnzPad, m_val.as<double>(), m_val32.as<float>()), "fp32 values");
+        m_val32Valid = true;
+    }
+    if (isSell(cfg) && !m_sell32Valid) {
+        alloc(m_sellVal32, sizeof(float) * ((size_t)m_sellTotal + 32), "sliced fp32 values");
+        check(sell_fill<float>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                               m_sliceOff.as<int>(), nullptr, m_sellVal32.as<float>()),
+              "sliced fp32 fill");
+        m_sell32Valid = true;
+    }
+}
+
+// The mixed solver's FP32 SpMV has no FP64 issue limit, so its best layout
+// and unroll can differ from the FP64 choice: every configuration is timed
+// again in FP32 (plain mode, median of 3) once per matrix structure.  With a
+// forced layout (XJPCG_SPMV_LANES / _CFG or xJPCG_gbSetSpmvLanes) the FP64
+// choice is kept.
+void PcgHandle::tuneSpmv32() {
+    if (m_tuned32Gen == m_structGen && m_spmvCfg32 >= 0) return;
+    const int ncfg = numSpmvCfgs();
+    const size_t vb32 = sizeof(float) * ((size_t)m_n4 + 4);
+    alloc(m_p32, vb32, "p32");
+    alloc(m_Ap32, vb32, "Ap32");
+    int best = m_spmvCfg;
+    m_tuneMs32.assign(ncfg, -1.f);
+    if (m_forcedLanes == 0 && envInt("XJPCG_SPMV_CFG", -1) < 0) {
+        float bestMs = 1e30f;
+        check(cudaMemsetAsync(m_p32.p, 0, vb32, m_stream), "memset");
+        for (int c = 0; c < ncfg; ++c) {
+            const int grid = spmvGrid32(c);
+            if (grid <= 0 || (isSell(c) && !ensureSell())) continue;
+            ensureValues32(c);
+            float ms[3];
+            for (int rep = 0; rep < 4; ++rep) {
+                check(cudaEventRecord(m_ev0, m_stream), "event");
+                check(spmv32(c, grid, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, m_state.as<CgState>(),
+                             m_partials.as<double>(), kSpmvPlain, nullptr),
+                      "SpMV fp32");
+                check(cudaEventRecord(m_ev1, m_stream), "event");
+                check(cudaEventSynchronize(m_ev1), "event");
+                if (rep > 0) check(cudaEventElapsedTime(&ms[rep - 1], m_ev0, m_ev1), "event");
+            }
+            std::sort(ms, ms + 3);
+            m_tuneMs32[c] = ms[1];
+            if (ms[1] < bestMs) {
+                bestMs = ms[1];
+                best = c;
+            }
+        }
+    }
+    m_spmvCfg32 = best;
+    m_spmvGrid32 = spmvGrid32(best);
+    m_tuned32Gen = m_structGen;
+    ++m_generation;  // the mixed graph embeds the configuration
+}
+
+int PcgHandle::tuning32(float* ms, int cap) const {
+    const int ncfg = numSpmvCfgs();
+    for (int c = 0; c < ncfg && c < cap; ++c) ms[c] = c < (int)m_tuneMs32.size() ? m_tuneMs32[c] : -1.f;
+    return ncfg;
 }
 
 // ---------------------------------------------------------------------------
@@ -622,8 +691,8 @@ void PcgHandle::buildMixedGraph() {
     const int n = (int)m_n, n4 = (int)m_n4;
     (void)n;
     const int vg = vec_grid(n4, m_numSms);
-    const int cfg32 = m_spmvCfg;
-    const int grid32 = spmvGrid32(cfg32);
+    const int cfg32 = m_spmvCfg32;
+    const int grid32 = m_spmvGrid32;
     CgState* st = m_state.as<CgState>();
     double* part = m_partials.as<double>();
     cudaGraph_t g = nullptr;
@@ -702,19 +771,8 @@ Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
     alloc(m_d32, vb32, "d32");
     alloc(m_Ap32, vb32, "Ap32");
     alloc(m_J32, vb32, "J32");
-    const uint64_t nnzPad = (m_nnz + 3) / 4 * 4 + 4;
-    if (!m_val32Valid) {
-        alloc(m_val32, sizeof(float) * nnzPad, "fp32 values");
-        check(convert_f64_to_f32(m_stream, (int64_t)nnzPad, m_val.as<double>(), m_val32.as<float>()), "fp32 values");
-        m_val32Valid = true;
-    }
-    if (isSell(m_spmvCfg) && !m_sell32Valid) {
-        alloc(m_sellVal32, sizeof(float) * ((size_t)m_sellTotal + 32), "sliced fp32 values");
-        check(sell_fill<float>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
-                               m_sliceOff.as<int>(), nullptr, m_sellVal32.as<float>()),
-              "sliced fp32 fill");
-        m_sell32Valid = true;
-    }
+    tuneSpmv32();
+    ensureValues32(m_spmvCfg32);
     check(cudaMemsetAsync(m_Ap32.p, 0, vb32, m_stream), "memset");
     CgState* st = m_state.as<CgState>();
     buildMixedGraph();
@@ -1245,6 +1303,10 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->batchSmemRows = (uint32_t)m_batchSmemRows;
     info->batchGrid = (uint32_t)m_batchGrid;
     info->batchMs = m_batchMs;
+    const int c32 = m_spmvCfg32 >= 0 ? m_spmvCfg32 : m_spmvCfg;
+    info->spmvLayout32 = isMerge(c32) ? 2u : (isSellNarrow(c32) ? 3u : (isSell(c32) ? 1u : 0u));
+    info->spmvCfg32 = m_spmvCfg32 >= 0 ? (uint32_t)m_spmvCfg32 : 0xffffffffu;
+    info->spmvCfg = (uint32_t)m_spmvCfg;
 }
 
 }  // namespace xjpcg

@@ -133,6 +133,7 @@ class PcgHandle {
     uint64_t getRecords(void* buf, uint64_t cap);
     void fillInfo(XJPCG_GbInfo_t* info) const;
     int tuning(float* ms, int* shape, int cap) const;
+    int tuning32(float* ms, int cap) const;
     void setLanes(int lanes);
 
     bool hasMatrix() const { return m_haveMatrix; }
@@ -165,6 +166,8 @@ class PcgHandle {
     int spmvGrid64(int cfg);
     int spmvGrid32(int cfg);
     bool ensureSell();
+    void ensureValues32(int cfg);
+    void tuneSpmv32();
     void refreshSellValues();
     cudaError_t spmv64(int cfg, int grid, const double* x, double* y, const double* b, CgState* st, double* part,
                        int mode, const uint32_t* done);
@@ -208,9 +211,13 @@ class PcgHandle {
     bool m_val32Valid = false;
     int m_forcedLanes = 0;
     int m_spmvCfg = 2;
-    int m_spmvGrid32Cfg = 2;
     int m_spmvGrid = 0;
     std::vector<float> m_tuneMs;  // median time of each SpMV configuration at the last tuning
+    // FP32 SpMV of the mixed solver: tuned separately (no FP64 issue limit)
+    int m_spmvCfg32 = -1;
+    int m_spmvGrid32 = 0;
+    uint64_t m_tuned32Gen = ~0ull;
+    std::vector<float> m_tuneMs32;
 
     // vectors
     uint32_t m_vecN = 0, m_n4 = 0;

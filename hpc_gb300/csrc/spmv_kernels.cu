@@ -505,7 +505,10 @@ template <typename VT, typename CT>
 void sell_kernel_launch(int u, int grid, cudaStream_t st, int n, int nslices, const int* sliceOff, const CT* scol,
                         const VT* sval, const VT* x, VT* y, const VT* b, CgState* state, double* partials, int mode,
                         const uint32_t* doneFlag) {
-    if (u == 4)
+    if (u == 16)
+        spmv_sell_kernel<VT, 16, CT><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
+                                                                   partials, mode, doneFlag);
+    else if (u == 4)
         spmv_sell_kernel<VT, 4, CT><<<grid, kSellThreads, 0, st>>>(n, nslices, sliceOff, scol, sval, x, y, b, state,
                                                                   partials, mode, doneFlag);
     else if (u == 8)
@@ -518,10 +521,10 @@ void sell_kernel_launch(int u, int grid, cudaStream_t st, int n, int nslices, co
 }  // namespace
 
 // Sliced configurations: 0-2 absolute int32 columns with unroll 4, 8, 2;
-// 3-4 int16 column offsets with unroll 4, 8.
-int sell_num_configs() { return 5; }
+// 3-5 int16 column offsets with unroll 4, 8, 16.
+int sell_num_configs() { return 6; }
 int sell_config_unroll(int cfg) {
-    static const int u[5] = {4, 8, 2, 4, 8};
+    static const int u[6] = {4, 8, 2, 4, 8, 16};
     return u[cfg];
 }
 bool sell_config_narrow(int cfg) { return cfg >= 3; }
@@ -582,7 +585,7 @@ int sell_grid(int cfg, int n, int numSms) {
     const int u = sell_config_unroll(cfg);
     int bps;
     if (sell_config_narrow(cfg))
-        bps = u == 4 ? sell_bps<VT, 4, int16_t>() : sell_bps<VT, 8, int16_t>();
+        bps = u == 4 ? sell_bps<VT, 4, int16_t>() : (u == 8 ? sell_bps<VT, 8, int16_t>() : sell_bps<VT, 16, int16_t>());
     else
         bps = u == 4 ? sell_bps<VT, 4, int>() : (u == 8 ? sell_bps<VT, 8, int>() : sell_bps<VT, 2, int>());
     if (bps <= 0) return 0;
@@ -603,6 +606,7 @@ cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const in
         sell_kernel_launch<VT, int16_t>(u, grid, st, n, nslices, sliceOff, scol16, sval, x, y, b, state, partials,
                                         mode, doneFlag);
     } else {
+        if (u == 16) return cudaErrorInvalidValue;  // no int32-column unroll-16 configuration
         sell_kernel_launch<VT, int>(u, grid, st, n, nslices, sliceOff, scol, sval, x, y, b, state, partials, mode,
                                     doneFlag);
     }

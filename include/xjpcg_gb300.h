@@ -39,6 +39,10 @@ typedef struct {
     uint32_t batchSmemRows;/* batched solves: rows of p held in shared memory */
     uint32_t batchGrid;    /* batched solves: CTAs of the persistent launch */
     double batchMs;        /* batched solves: device time of the last batch (CUDA events) */
+    uint32_t spmvCfg;      /* index of the FP64 SpMV configuration in the tuning table */
+    uint32_t spmvCfg32;    /* index of the mixed solver's FP32 SpMV configuration (~0 until tuned) */
+    uint32_t spmvLayout32; /* layout of that configuration, coded as spmvLayout */
+    uint32_t reserved;
 } XJPCG_GbInfo_t;
 
 /* Per-system outcome of a batched solve. */
@@ -188,13 +192,20 @@ XJPCG_Status_t xJPCG_gbGetInfo(const XJPCG_Handle_t* handle, XJPCG_GbInfo_t* inf
 XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, int32_t* shape, int32_t cap,
                                      int32_t* count);
 
+/* FP32 SpMV tuner report of the mixed solver (same configuration order as
+ * xJPCG_gbGetSpmvTuning): ms[c] = median time of a plain FP32 SpMV, -1 when
+ * not timed (not yet tuned, configuration not available, or a forced
+ * layout).  At most cap entries are written. */
+XJPCG_Status_t xJPCG_gbGetSpmvTuning32(const XJPCG_Handle_t* handle, float* ms, int32_t cap, int32_t* count);
+
 /* The cudaStream_t the handle launches on (for event timing by callers). */
 XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream);
 
 /* Forces the CSR SpMV lanes-per-row (1, 2, 4, 8, 16, 32); -1 forces the
  * sliced layout, -2 the merge-path kernel, -3 the sliced layout with int16
- * column offsets (INVALID_VALUE at the next solve when some column lies more
- * than 32767 from its row); 0 restores tuning. */
+ * column offsets (INVALID_VALUE when some column lies more than 32767 from
+ * its row); 0 restores tuning.  A forced layout applies to the FP32 SpMV of
+ * the mixed solver as well. */
 XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes);
 
 /* y = A x and *d_dot = x.y for callers that cannot allocate device memory.
