@@ -782,7 +782,7 @@ Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
     cmd.useCond = 1;
     cmd.condHandle = (uint64_t)m_condOuter;
     cmd.relHandle = (uint64_t)m_condInner;
-    const double delta = envDouble("XJPCG_RELIABLE_DELTA", 0.1);
+    const double delta = envDouble("XJPCG_RELIABLE_DELTA", 0.01);
     cmd.delta2 = delta * delta;
     check(cudaMemcpyAsync(st, &cmd, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
     check(cudaEventRecord(m_ev0, m_stream), "event");

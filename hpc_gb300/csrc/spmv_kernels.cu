@@ -426,9 +426,17 @@ __device__ __forceinline__ int sell_column<int16_t>(const int16_t* p, int base) 
     return base + (int)__ldcs(reinterpret_cast<const short*>(p));
 }
 
+// Resident CTAs per SM the register budget is set for: FP64 needs 40
+// registers (6 CTAs); FP32 with unroll >= 8, which has no FP64 issue limit,
+// fits 32 registers without spilling and gets the full 64 warps (8 CTAs).
+template <typename VT, int U>
+struct SellMinBlocks {
+    static constexpr int value = (sizeof(VT) == 4 && U >= 8) ? 8 : 6;
+};
+
 // CT = int: absolute columns; CT = int16_t: offsets from the row.
 template <typename VT, int U, typename CT>
-__global__ void __launch_bounds__(kSellThreads, 6) spmv_sell_kernel(int n, int nslices, const int* __restrict__ sliceOff,
+__global__ void __launch_bounds__(kSellThreads, SellMinBlocks<VT, U>::value) spmv_sell_kernel(int n, int nslices, const int* __restrict__ sliceOff,
                                                                  const CT* __restrict__ scol,
                                                                  const VT* __restrict__ sval, const VT* __restrict__ x,
                                                                  VT* __restrict__ y, const VT* __restrict__ b,

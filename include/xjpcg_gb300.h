@@ -68,12 +68,16 @@ XJPCG_Status_t xJPCG_gbCsrSolver(XJPCG_Handle_t* handle, uint32_t n, uint32_t nn
 XJPCG_Status_t xJPCG_gbSolveDevice(XJPCG_Handle_t* handle, const double* d_b, const double* d_diagA, double* d_x,
                                    uint32_t maxIter, double tol, uint32_t* iter, double* res);
 
-/* Mixed precision solve with the stored matrix: FP32 Jacobi-PCG inner loop
- * (FP32 values, vectors and accumulation) inside an FP64 iterative
- * refinement loop that recomputes r = b - A x in FP64 and updates x in FP64.
- * Stops when ||b - A x|| <= tol ||b|| (true residual) or after maxIter inner
- * iterations in total.  *iter = inner iterations, *res = final true relative
- * residual.  onDevice != 0: b, diagA and x are device pointers. */
+/* Mixed precision solve with the stored matrix (reliable updates): the CG
+ * recurrences run in FP32 (FP32 values, vectors and dot products) and keep
+ * their search direction; a refresh folds the FP32 correction into the FP64
+ * x, recomputes r = b - A x with an FP64 SpMV and restarts the FP32 residual
+ * from it.  A refresh runs when the FP32 residual norm has fallen by a factor
+ * delta below its largest value since the last refresh (delta = 0.01, or
+ * XJPCG_RELIABLE_DELTA), when it meets the tolerance, and when the iteration
+ * budget runs out.  Stops when ||b - A x|| <= tol ||b|| (true FP64 residual)
+ * or after maxIter iterations.  *iter = FP32 iterations, *res = final true
+ * relative residual.  onDevice != 0: b, diagA and x are device pointers. */
 XJPCG_Status_t xJPCG_gbMixedSolve(XJPCG_Handle_t* handle, const double* b, const double* diagA, double* x,
                                   uint32_t maxIter, double tol, uint32_t* iter, double* res, int onDevice);
 
