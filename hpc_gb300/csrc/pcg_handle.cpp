@@ -254,6 +254,8 @@ void PcgHandle::finishMatrix() {
     m_val32Valid = false;
     m_sellState = 0;
     m_sell32Valid = false;
+    m_ssState = 0;
+    m_ss32Valid = false;
     m_mergeTilesValid = false;
     ++m_structGen;
     check(cudaStreamSynchronize(m_stream), "sync");
@@ -267,19 +269,30 @@ void PcgHandle::setLanes(int lanes) {
     if (m_haveMatrix) tuneSpmv();
 }
 
-// Picks the lanes-per-row shape by timing every SpMV configuration on the
-// stored matrix (plain mode, x = p buffer), median of three launches each.
+// Picks the SpMV configuration by timing every one on the stored matrix
+// (plain mode, x = p buffer), median of three launches each.
 void PcgHandle::refreshSellValues() {
     m_sell32Valid = false;
-    if (m_sellState != 1) return;
-    check(sell_fill<double>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
-                            m_sliceOff.as<int>(), nullptr, m_sellVal.as<double>()),
-          "sliced fill");
+    m_ss32Valid = false;
+    if (m_sellState == 1)
+        check(sell_fill<double>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                                m_sliceOff.as<int>(), nullptr, m_sellVal.as<double>()),
+              "sliced fill");
+    if (m_ssState == 1)
+        check(sellsort_fill<double>(m_stream, (int)m_n, m_ssLong, m_rowptr.as<int>(), m_col.as<int>(),
+                                    m_val.as<double>(), m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), nullptr,
+                                    m_ssVal.as<double>()),
+              "sorted sliced fill");
 }
 
 // Configuration index space: [0, ncsr) staged CSR shapes, [ncsr, ncsr +
-// nsell) sliced unroll depths, ncsr + nsell the merge-path kernel.
-int PcgHandle::numSpmvCfgs() const { return spmv_num_configs() + sell_num_configs() + 1; }
+// nsell) sliced unroll depths, then the sorted-sliced unroll depths, then the
+// merge-path kernel.
+int PcgHandle::numSpmvCfgs() const { return mergeCfg() + 1; }
+
+int PcgHandle::sortedCfg0() const { return spmv_num_configs() + sell_num_configs(); }
+
+int PcgHandle::mergeCfg() const { return sortedCfg0() + sellsort_num_configs(); }
 
 bool PcgHandle::isSell(int cfg) const {
     return cfg >= spmv_num_configs() && cfg < spmv_num_configs() + sell_num_configs();
@@ -287,7 +300,59 @@ bool PcgHandle::isSell(int cfg) const {
 
 bool PcgHandle::isSellNarrow(int cfg) const { return isSell(cfg) && sell_config_narrow(cfg - spmv_num_configs()); }
 
-bool PcgHandle::isMerge(int cfg) const { return cfg == spmv_num_configs() + sell_num_configs(); }
+bool PcgHandle::isSorted(int cfg) const { return cfg >= sortedCfg0() && cfg < mergeCfg(); }
+
+bool PcgHandle::isMerge(int cfg) const { return cfg == mergeCfg(); }
+
+uint32_t PcgHandle::layoutCode(int cfg) const {
+    if (isMerge(cfg)) return 2u;
+    if (isSorted(cfg)) return 4u;
+    if (isSellNarrow(cfg)) return 3u;
+    return isSell(cfg) ? 1u : 0u;
+}
+
+// Builds (once per matrix) the length-sorted sliced copy.  Only offered when
+// the plain sliced layout is rejected or pads more than 20 %: for matrices
+// with near-uniform rows sorting buys nothing and costs set-up time.
+bool PcgHandle::ensureSorted() {
+    if (m_ssState == 1) return true;
+    if (m_ssState == 2) return false;
+    if (ensureSell() && m_sellPadRatio <= 1.2) {
+        m_ssState = 2;
+        return false;
+    }
+    const int n = (int)m_n;
+    const int tiles = sellsort_tiles(n);
+    const int binsTotal = sellsort_bins() * tiles;
+    alloc(m_ssSorted, sizeof(int) * ((size_t)n + 32), "sorted rows");
+    alloc(m_ssHist, sizeof(int) * ((size_t)binsTotal + 1), "sorted-row histogram");
+    alloc(m_ssStart, sizeof(int) * ((size_t)binsTotal + 1), "sorted-row histogram");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count(std::max(binsTotal, n) + 1) + 16), "scan scratch");
+    int nLong = 0;
+    check(sellsort_order(m_stream, n, m_rowptr.as<int>(), m_ssHist.as<int>(), m_ssStart.as<int>(),
+                         m_blockSums.as<int>(), m_ssSorted.as<int>(), &nLong),
+          "row sort");
+    const int nSlices = (n - nLong + 31) / 32;
+    alloc(m_ssSliceOff, sizeof(int) * ((size_t)nSlices + 1), "sorted slice offsets");
+    int64_t total = 0;
+    check(sellsort_slices(m_stream, n, nLong, m_rowptr.as<int>(), m_ssSorted.as<int>(), m_ssSliceOff.as<int>(),
+                          m_blockSums.as<int>(), &total),
+          "sorted slices");
+    if (total > 0x7fffff00ll) {
+        m_ssState = 2;
+        return false;
+    }
+    alloc(m_ssCol, sizeof(int) * ((size_t)total + 32), "sorted sliced columns");
+    alloc(m_ssVal, sizeof(double) * ((size_t)total + 32), "sorted sliced values");
+    check(sellsort_fill<double>(m_stream, n, nLong, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                                m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), m_ssCol.as<int>(), m_ssVal.as<double>()),
+          "sorted sliced fill");
+    m_ssLong = nLong;
+    m_ssTotal = total;
+    m_ssState = 1;
+    m_ss32Valid = false;
+    return true;
+}
 
 void PcgHandle::ensureMergeScratch() {
     const int nt = merge_tiles((int)m_n, (int64_t)m_nnz);
@@ -305,6 +370,8 @@ int PcgHandle::spmvGrid64(int cfg) {
         ensureMergeScratch();
         return merge_tiles((int)m_n, (int64_t)m_nnz);
     }
+    if (isSorted(cfg))
+        return ensureSorted() ? sellsort_grid<double>(cfg - sortedCfg0(), (int)m_n, m_ssLong, m_numSms) : 0;
     if (!isSell(cfg)) return spmv_grid<double>(cfg, (int)m_n, m_numSms);
     if (!ensureSell() || (isSellNarrow(cfg) && !m_sellNarrow)) return 0;
     return sell_grid<double>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
@@ -315,6 +382,8 @@ int PcgHandle::spmvGrid32(int cfg) {
         ensureMergeScratch();
         return merge_tiles((int)m_n, (int64_t)m_nnz);
     }
+    if (isSorted(cfg))
+        return ensureSorted() ? sellsort_grid<float>(cfg - sortedCfg0(), (int)m_n, m_ssLong, m_numSms) : 0;
     if (!isSell(cfg)) return spmv_grid<float>(cfg, (int)m_n, m_numSms);
     if (isSellNarrow(cfg) && !m_sellNarrow) return 0;
     return sell_grid<float>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
@@ -331,6 +400,11 @@ cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, con
         if (e != cudaSuccess || mode != kSpmvResidual) return e;
         return residual_finish_launch<double>(m_stream, (int)m_n, b, y, part, st);
     }
+    if (isSorted(cfg))
+        return spmv_sellsort_launch<double>(cfg - sortedCfg0(), grid, m_stream, (int)m_n, m_ssLong,
+                                            m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), m_ssCol.as<int>(),
+                                            m_ssVal.as<double>(), m_rowptr.as<int>(), m_col.as<int>(),
+                                            m_val.as<double>(), x, y, b, st, part, mode, done);
     if (!isSell(cfg))
         return spmv_launch<double>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
                                    m_val.as<double>(), x, y, b, st, part, mode, done);
@@ -346,6 +420,11 @@ cudaError_t PcgHandle::spmv32(int cfg, int grid, const float* x, float* y, const
                                         m_val32.as<float>(), x, y, m_mergeTile.as<int>(), m_mergeRow.as<int>(),
                                         m_mergeVal.p,
                                         m_mergePart.as<double>(), st, mode, done);
+    if (isSorted(cfg))
+        return spmv_sellsort_launch<float>(cfg - sortedCfg0(), grid, m_stream, (int)m_n, m_ssLong,
+                                           m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), m_ssCol.as<int>(),
+                                           m_ssVal32.as<float>(), m_rowptr.as<int>(), m_col.as<int>(),
+                                           m_val32.as<float>(), x, y, b, st, part, mode, done);
     if (!isSell(cfg))
         return spmv_launch<float>(cfg, grid, m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(),
                                   m_val32.as<float>(), x, y, b, st, part, mode, done);
@@ -374,6 +453,7 @@ bool PcgHandle::ensureSell() {
           "D2H");
     check(cudaStreamSynchronize(m_stream), "sync");
     const int64_t phantom = (int64_t)(nslices * 32 - (int64_t)m_n) * ((total - lastOff) / 32);
+    m_sellPadRatio = (double)(total - phantom) / (double)std::max<uint64_t>(m_nnz, 1);
     if ((uint64_t)(total - phantom) > m_nnz + m_nnz / 2 + 64 || total > 0x7fffff00ll) {
         m_sellState = 2;
         return false;
@@ -407,7 +487,11 @@ void PcgHandle::tuneSpmv() {
     if (forcedCfg >= 0 && forcedCfg < ncfg) {
         best = forcedCfg;
     } else if (m_forcedLanes == -2) {
-        best = spmv_num_configs() + sell_num_configs();
+        best = mergeCfg();
+    } else if (m_forcedLanes == -4) {
+        if (!ensureSorted())
+            throw InvalidValue("the length-sorted sliced SpMV layout is not offered for this matrix.");
+        best = sortedCfg0() + 1;  // unroll 8
     } else if (m_forcedLanes == -3) {
         if (!ensureSell() || !m_sellNarrow)
             throw InvalidValue("the sliced SpMV layout with 16-bit column offsets is not available for this matrix.");
@@ -425,7 +509,11 @@ void PcgHandle::tuneSpmv() {
         for (int c = 0; c < ncfg; ++c) {
             const int grid = spmvGrid64(c);
             if (grid <= 0) continue;
+            // one warm-up launch, then up to three timed ones; a configuration
+            // whose first timed launch is more than twice the best so far
+            // is not timed further (it keeps that one time)
             float ms[3];
+            int timed = 0;
             for (int rep = 0; rep < 4; ++rep) {
                 check(cudaEventRecord(m_ev0, m_stream), "event");
                 check(spmv64(c, grid, m_p.as<double>(), m_Ap.as<double>(), nullptr,
@@ -433,12 +521,13 @@ void PcgHandle::tuneSpmv() {
                       "SpMV");
                 check(cudaEventRecord(m_ev1, m_stream), "event");
                 check(cudaEventSynchronize(m_ev1), "event");
-                if (rep > 0) check(cudaEventElapsedTime(&ms[rep - 1], m_ev0, m_ev1), "event");
+                if (rep > 0) check(cudaEventElapsedTime(&ms[timed++], m_ev0, m_ev1), "event");
+                if (rep == 1 && ms[0] > 2.f * bestMs) break;
             }
-            std::sort(ms, ms + 3);
-            m_tuneMs[c] = ms[1];
-            if (ms[1] < bestMs) {
-                bestMs = ms[1];
+            std::sort(ms, ms + timed);
+            m_tuneMs[c] = ms[timed / 2];
+            if (ms[timed / 2] < bestMs) {
+                bestMs = ms[timed / 2];
                 best = c;
             }
         }
@@ -458,6 +547,13 @@ void PcgHandle::ensureValues32(int cfg) {
         alloc(m_val32, sizeof(float) * nnzPad, "fp32 values");
         check(convert_f64_to_f32(m_stream, (int64_t)nnzPad, m_val.as<double>(), m_val32.as<float>()), "fp32 values");
         m_val32Valid = true;
+    }
+    if (isSorted(cfg) && !m_ss32Valid) {
+        alloc(m_ssVal32, sizeof(float) * ((size_t)m_ssTotal + 32), "sorted sliced fp32 values");
+        check(sellsort_fill<float>(m_stream, (int)m_n, m_ssLong, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                                   m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), nullptr, m_ssVal32.as<float>()),
+              "sorted sliced fp32 fill");
+        m_ss32Valid = true;
     }
     if (isSell(cfg) && !m_sell32Valid) {
         alloc(m_sellVal32, sizeof(float) * ((size_t)m_sellTotal + 32), "sliced fp32 values");
@@ -489,6 +585,7 @@ void PcgHandle::tuneSpmv32() {
             if (grid <= 0 || (isSell(c) && !ensureSell())) continue;
             ensureValues32(c);
             float ms[3];
+            int timed = 0;
             for (int rep = 0; rep < 4; ++rep) {
                 check(cudaEventRecord(m_ev0, m_stream), "event");
                 check(spmv32(c, grid, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, m_state.as<CgState>(),
@@ -496,12 +593,13 @@ void PcgHandle::tuneSpmv32() {
                       "SpMV fp32");
                 check(cudaEventRecord(m_ev1, m_stream), "event");
                 check(cudaEventSynchronize(m_ev1), "event");
-                if (rep > 0) check(cudaEventElapsedTime(&ms[rep - 1], m_ev0, m_ev1), "event");
+                if (rep > 0) check(cudaEventElapsedTime(&ms[timed++], m_ev0, m_ev1), "event");
+                if (rep == 1 && ms[0] > 2.f * bestMs) break;
             }
-            std::sort(ms, ms + 3);
-            m_tuneMs32[c] = ms[1];
-            if (ms[1] < bestMs) {
-                bestMs = ms[1];
+            std::sort(ms, ms + timed);
+            m_tuneMs32[c] = ms[timed / 2];
+            if (ms[timed / 2] < bestMs) {
+                bestMs = ms[timed / 2];
                 best = c;
             }
         }
@@ -1264,6 +1362,12 @@ int PcgHandle::tuning(float* ms, int* shape, int cap) const {
             shape[4 * c + 1] = 256;
             shape[4 * c + 2] = merge_items_per_thread();
             shape[4 * c + 3] = 0;
+        } else if (isSorted(c)) {
+            // length-sorted sliced layout: (1, 1, unroll, 32)
+            shape[4 * c] = 1;
+            shape[4 * c + 1] = 1;
+            shape[4 * c + 2] = sellsort_config_unroll(c - sortedCfg0());
+            shape[4 * c + 3] = 32;
         } else if (isSell(c)) {
             // sliced layout: one lane per row, no CTA staging; chunk = unroll,
             // last field = bits per stored column (32 absolute, 16 offset)
@@ -1285,7 +1389,7 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->nnz = m_nnz;
     info->itersRun = m_lastState.k;
     info->spmvLanes = isMerge(m_spmvCfg) ? 0u : (isSell(m_spmvCfg) ? 1u : (uint32_t)spmv_config_lanes(m_spmvCfg));
-    info->spmvLayout = isMerge(m_spmvCfg) ? 2u : (isSellNarrow(m_spmvCfg) ? 3u : (isSell(m_spmvCfg) ? 1u : 0u));
+    info->spmvLayout = layoutCode(m_spmvCfg);
     info->spmvGrid = (uint32_t)m_spmvGrid;
     info->statusBits = m_lastState.status;
     info->outerSweeps = m_lastOuter;
@@ -1304,7 +1408,7 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->batchGrid = (uint32_t)m_batchGrid;
     info->batchMs = m_batchMs;
     const int c32 = m_spmvCfg32 >= 0 ? m_spmvCfg32 : m_spmvCfg;
-    info->spmvLayout32 = isMerge(c32) ? 2u : (isSellNarrow(c32) ? 3u : (isSell(c32) ? 1u : 0u));
+    info->spmvLayout32 = layoutCode(c32);
     info->spmvCfg32 = m_spmvCfg32 >= 0 ? (uint32_t)m_spmvCfg32 : 0xffffffffu;
     info->spmvCfg = (uint32_t)m_spmvCfg;
 }

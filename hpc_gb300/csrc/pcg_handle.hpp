@@ -161,6 +161,11 @@ class PcgHandle {
     int numSpmvCfgs() const;
     bool isSell(int cfg) const;
     bool isSellNarrow(int cfg) const;
+    bool isSorted(int cfg) const;
+    int sortedCfg0() const;
+    int mergeCfg() const;
+    uint32_t layoutCode(int cfg) const;
+    bool ensureSorted();
     bool isMerge(int cfg) const;
     void ensureMergeScratch();
     int spmvGrid64(int cfg);
@@ -202,6 +207,13 @@ class PcgHandle {
     DevBuf m_sliceOff, m_sellCol, m_sellVal, m_sellVal32;
     DevBuf m_sellCol16;          // int16 column offsets (when the matrix is narrow enough)
     bool m_sellNarrow = false;
+    double m_sellPadRatio = 0.0;  // stored / real entries of the sliced copy
+    // length-sorted sliced copy (irregular rows)
+    DevBuf m_ssSorted, m_ssHist, m_ssStart, m_ssSliceOff, m_ssCol, m_ssVal, m_ssVal32;
+    int m_ssState = 0;  // 0 not built, 1 built, 2 not offered
+    int m_ssLong = 0;
+    int64_t m_ssTotal = 0;
+    bool m_ss32Valid = false;
     int m_sellState = 0;  // 0 not built, 1 built, 2 rejected (too much padding)
     DevBuf m_mergeRow, m_mergeVal, m_mergePart;  // merge-path carries and partials
     DevBuf m_mergeTile;                          // merge-path tile start rows

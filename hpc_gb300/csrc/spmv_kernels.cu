@@ -426,12 +426,11 @@ __device__ __forceinline__ int sell_column<int16_t>(const int16_t* p, int base) 
     return base + (int)__ldcs(reinterpret_cast<const short*>(p));
 }
 
-// Resident CTAs per SM the register budget is set for: FP64 needs 40
-// registers (6 CTAs); FP32 with unroll >= 8, which has no FP64 issue limit,
-// fits 32 registers without spilling and gets the full 64 warps (8 CTAs).
+// Resident CTAs per SM the register budget is set for: 6 (40 registers).
+// An FP32 build capped at 32 registers (8 CTAs) measured slower.
 template <typename VT, int U>
 struct SellMinBlocks {
-    static constexpr int value = (sizeof(VT) == 4 && U >= 8) ? 8 : 6;
+    static constexpr int value = 6;
 };
 
 // CT = int: absolute columns; CT = int16_t: offsets from the row.

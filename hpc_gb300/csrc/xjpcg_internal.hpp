@@ -43,6 +43,28 @@ cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const in
                              const int16_t* scol16, const VT* sval, const VT* x, VT* y, const VT* b, CgState* state,
                              double* partials, int mode, const uint32_t* doneFlag);
 
+// ---- length-sorted sliced SpMV (spmv_sellsort.cu) ----
+int sellsort_num_configs();
+int sellsort_config_unroll(int cfg);
+int sellsort_tiles(int n);
+int sellsort_bins();
+// hist/start: sellsort_bins() * sellsort_tiles(n) ints each; sorted: n ints.
+cudaError_t sellsort_order(cudaStream_t st, int n, const int* rowptr, int* hist, int* start, int* blockSums,
+                           int* sorted, int* nLong);
+// sliceOff: (n - nLong + 31) / 32 + 1 ints; *total = stored slice entries.
+cudaError_t sellsort_slices(cudaStream_t st, int n, int nLong, const int* rowptr, const int* sorted, int* sliceOff,
+                            int* blockSums, int64_t* total);
+template <typename VT>
+cudaError_t sellsort_fill(cudaStream_t st, int n, int nLong, const int* rowptr, const int* col, const double* val,
+                          const int* sorted, const int* sliceOff, int* scol, VT* sval);
+template <typename VT>
+int sellsort_grid(int cfg, int n, int nLong, int numSms);
+template <typename VT>
+cudaError_t spmv_sellsort_launch(int cfg, int grid, cudaStream_t st, int n, int nLong, const int* sorted,
+                                 const int* sliceOff, const int* scol, const VT* sval, const int* rowptr,
+                                 const int* col, const VT* val, const VT* x, VT* y, const VT* b, CgState* state,
+                                 double* partials, int mode, const uint32_t* doneFlag);
+
 // ---- merge-path SpMV (spmv_merge.cu) ----
 // Scratch per matrix: tileRow[ntiles + 1] ints (merge_partition), carryRow[ntiles] ints, carryVal[ntiles] accumulators
 // (double for fp64, float for fp32), partials[ntiles + merge_fixup_grid(ntiles)].

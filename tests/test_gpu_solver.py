@@ -376,3 +376,52 @@ def test_mixed_precision_small(handle):
     err64 = np.linalg.norm(r64.x - tight["x"]) / np.linalg.norm(tight["x"])
     assert err <= max(10 * err64, 1e-8), (err, err64)
     assert handle.info().outerSweeps >= 1
+
+
+@pytest.fixture(scope="module")
+def zipf_small():
+    # power-law rows (4 .. 1500 entries): the plain sliced layout pads too
+    # much, so the length-sorted sliced layout is offered
+    return W.zipf_spd(30000, hi=1500, seed=5)
+
+
+def test_sorted_sliced_spmv_and_solve(handle, zipf_small):
+    s = zipf_small
+    handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
+    handle.set_spmv_lanes(-4)
+    assert handle.info().spmvLayout == 4
+    x = np.random.default_rng(3).standard_normal(s.n)
+    y = handle.spmv(x)
+    yref = oracle.spmv(s.rowptr, s.col, s.val, x)
+    scale = oracle.spmv(s.rowptr, s.col, np.abs(s.val), np.abs(x))
+    assert np.all(np.abs(y - yref) <= 1e-13 * scale)
+    r = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    _check_solve(s, r)
+    # the mixed solver follows the forced layout for its FP32 SpMV
+    m = handle.mixed_solve(s.b, s.diag, 20000, 1e-10)
+    assert m.status == X.SUCCESS and handle.info().spmvLayout32 == 4
+    assert oracle.true_relres(s.rowptr, s.col, s.val, s.b, m.x) <= 1e-10
+
+
+def test_sorted_sliced_deterministic_across_handles(zipf_small):
+    s = zipf_small
+    out = []
+    for _ in range(2):
+        h = X.JPCG()
+        try:
+            h.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
+            h.set_spmv_lanes(-4)
+            r = h.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10, mode=X.MODE_KEEP_MATRIX)
+            out.append((r.iters, r.x.copy()))
+        finally:
+            h.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_sorted_sliced_not_offered_for_uniform_rows(handle):
+    s = W.diffusion27(10, seed=2)
+    handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
+    with pytest.raises(X.XJPCGError):
+        handle.set_spmv_lanes(-4)
+    handle.set_spmv_lanes(0)
