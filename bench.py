@@ -50,9 +50,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the mixed-precision, batched and adjoint measurements")
-    ap.add_argument("--profile", choices=["spmv", "solve"], default=None,
+    ap.add_argument("--profile", choices=["spmv", "solve", "mixed"], default=None,
                     help="profiling driver for ncu: set the matrix, then run --reps plain SpMVs "
-                         "(spmv) or one resident solve (solve); no timing line")
+                         "(spmv), one resident fp64 solve (solve) or one mixed solve (mixed); no timing line")
     ap.add_argument("--workload", choices=["diffusion27", "zipf"], default="diffusion27",
                     help="matrix of --profile: diffusion27(--nx) or the 2M-row Zipf SPD system")
     ap.add_argument("--reps", type=int, default=4)
@@ -140,9 +140,9 @@ def committed_traffic(layout):
 
 def run_profile(args):
     """Profiling driver: the matrix is set through xJPCG_cooSolver (maxIter 0),
-    then --reps plain SpMVs (xJPCG_gbSpmv on device vectors) or one resident
-    solve (xJPCG_gbSolveDevice).  XJPCG_SPMV_LANES forces a layout and skips
-    the tuner's launches."""
+    then --reps plain SpMVs (xJPCG_gbSpmv on device vectors), one resident
+    solve (xJPCG_gbSolveDevice) or one mixed solve (xJPCG_gbMixedSolve).
+    XJPCG_SPMV_LANES forces a layout and skips the tuner's launches."""
     import torch
     import hpc_gb300 as X
     from hpc_gb300 import workloads as W
@@ -158,10 +158,16 @@ def run_profile(args):
     if args.profile == "spmv":
         for _ in range(args.reps):
             h.spmv(d_b.data_ptr(), d_y.data_ptr(), on_device=True)
-    else:
+    elif args.profile == "solve":
         d_diag = torch.from_numpy(sysm.diag).cuda()
         st, it, res = h.solve_device(d_b.data_ptr(), d_diag.data_ptr(), d_y.data_ptr(), 20000, 1e-10)
         print("solve status=%d iters=%d res=%.3e" % (st, it, res), flush=True)
+    else:
+        d_diag = torch.from_numpy(sysm.diag).cuda()
+        m = h.mixed_solve(d_b.data_ptr(), d_diag.data_ptr(), 20000, 1e-10, x=d_y.data_ptr(), on_device=True)
+        inf = h.info()
+        print("mixed status=%d iters=%d refreshes=%d res=%.3e layout32=%s" % (
+            m.status, m.iters, inf.outerSweeps, m.res, LAYOUTS[inf.spmvLayout32][0]), flush=True)
     torch.cuda.synchronize()
     h.close()
 
@@ -429,10 +435,14 @@ def run_gb300(args):
             e2e_step()
         torch.cuda.synchronize()
         te = max_over_ranks(time.perf_counter() - t0)
+        met, inf_e = h.metrics(), h.info()
         e2e = {"value": world * args.steps / te, "unit": "solves/s",
                "h2d_bytes_per_step": int(4 * nnz + 4 * nnz + 8 * nnz + 8 * n + 8 * n),
                "d2h_bytes_per_step": int(8 * n + 256), "time_to_tol_s": te / args.steps,
-               "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays"}
+               "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays",
+               "last_call_phases_s": {"matProc (H2D, conversion, layouts, tuning)": met.m_matProc,
+                                      "of which SpMV tuning": inf_e.tuneMs / 1e3,
+                                      "vecProc": met.m_vecProc, "solver (incl. D2H of x)": met.m_solver}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

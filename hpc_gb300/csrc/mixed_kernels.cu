@@ -26,6 +26,10 @@
 //       SpMV fp64, kResidual        r64 = b - A x, ||r64||^2
 //       rel_restart                 r = r64, r.z, beta, stop test
 //     rel_pupdate                   p = J r + beta p
+// Without graphs (XJPCG_HOST_LOOP=1, for profilers) the host launches the six
+// kernels of every iteration in batches; the refresh kernels then return at
+// once unless the update kernel chose a refresh (reliable / skipRefresh),
+// and every kernel returns once done is set.
 #include "xjpcg_device.cuh"
 #include "xjpcg_internal.hpp"
 
@@ -134,6 +138,7 @@ __global__ void __launch_bounds__(kMxThreads) rel_update_kernel(int n4, float* _
         // true residual).
         const bool refresh = bd || rrN < st->delta2 * st->rrMax || rrN < st->tols || k + 1u >= st->maxIterP1;
         st->reliable = refresh ? 1u : 0u;
+        st->skipRefresh = refresh ? 0u : 1u;
         if (bd) {
             st->status |= kStatusBreakdown;
         } else if (!refresh) {
@@ -146,7 +151,7 @@ __global__ void __launch_bounds__(kMxThreads) rel_update_kernel(int n4, float* _
 
 __global__ void __launch_bounds__(kMxThreads) rel_fold_kernel(int n4, double* __restrict__ x, float* __restrict__ d,
                                                               const CgState* st) {
-    if (!*(volatile const uint32_t*)&st->reliable) return;
+    if (!*(volatile const uint32_t*)&st->reliable || *(volatile const uint32_t*)&st->done) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
         x[i] += (double)d[i];
         d[i] = 0.f;
@@ -156,7 +161,7 @@ __global__ void __launch_bounds__(kMxThreads) rel_fold_kernel(int n4, double* __
 __global__ void __launch_bounds__(kMxThreads) rel_restart_kernel(int n4, const double* __restrict__ r64,
                                                                  const float* __restrict__ J, float* __restrict__ r,
                                                                  CgState* st, double* partials) {
-    if (!*(volatile uint32_t*)&st->reliable) return;
+    if (!*(volatile uint32_t*)&st->reliable || *(volatile uint32_t*)&st->done) return;
     float rz = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
         const float ri = (float)r64[i];
@@ -182,6 +187,7 @@ __global__ void __launch_bounds__(kMxThreads) rel_restart_kernel(int n4, const d
             st->rz = rzN;
         }
         st->done = stop ? 1u : 0u;
+        if (stop) st->skipRefresh = 1u;
         if (st->useCond && stop) cudaGraphSetConditional((cudaGraphConditionalHandle)st->condHandle, 0u);
     }
 }

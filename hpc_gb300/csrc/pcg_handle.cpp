@@ -398,7 +398,7 @@ cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, con
                                                   m_mergeRow.as<int>(), m_mergeVal.p,
                                                   m_mergePart.as<double>(), st, m, done);
         if (e != cudaSuccess || mode != kSpmvResidual) return e;
-        return residual_finish_launch<double>(m_stream, (int)m_n, b, y, part, st);
+        return residual_finish_launch<double>(m_stream, (int)m_n, b, y, part, st, done);
     }
     if (isSorted(cfg))
         return spmv_sellsort_launch<double>(cfg - sortedCfg0(), grid, m_stream, (int)m_n, m_ssLong,
@@ -479,7 +479,57 @@ bool PcgHandle::ensureSell() {
     return true;
 }
 
+// Times the SpMV configurations (plain mode, x = p, FP64 or FP32) and returns
+// the fastest.  Sliced layouts go first: on matrices they suit they are the
+// fastest, and a good early time lets the rest be judged quickly.  Each
+// configuration gets one launch (warm-up, timed); one that is over twice the
+// best so far keeps that time, the others get three more and keep the median.
+int PcgHandle::timeConfigs(bool fp32, std::vector<float>& out) {
+    const int ncfg = numSpmvCfgs();
+    std::vector<int> order;
+    for (int c = spmv_num_configs(); c < ncfg; ++c) order.push_back(c);
+    for (int c = 0; c < spmv_num_configs(); ++c) order.push_back(c);
+    int best = -1;
+    float bestMs = 1e30f;
+    for (int c : order) {
+        const int grid = fp32 ? spmvGrid32(c) : spmvGrid64(c);
+        if (grid <= 0) continue;
+        if (fp32) ensureValues32(c);
+        float ms[4];
+        int timed = 0;
+        for (int rep = 0; rep < 4; ++rep) {
+            check(cudaEventRecord(m_ev0, m_stream), "event");
+            check(fp32 ? spmv32(c, grid, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, m_state.as<CgState>(),
+                                m_partials.as<double>(), kSpmvPlain, nullptr)
+                       : spmv64(c, grid, m_p.as<double>(), m_Ap.as<double>(), nullptr, m_state.as<CgState>(),
+                                m_partials.as<double>(), kSpmvPlain, nullptr),
+                  "SpMV");
+            check(cudaEventRecord(m_ev1, m_stream), "event");
+            check(cudaEventSynchronize(m_ev1), "event");
+            check(cudaEventElapsedTime(&ms[timed++], m_ev0, m_ev1), "event");
+            if (rep == 0 && ms[0] > 2.f * bestMs) break;
+        }
+        float t = ms[0];
+        if (timed == 4) {  // median of the three launches after the warm-up
+            std::sort(ms + 1, ms + 4);
+            t = ms[2];
+        }
+        out[c] = t;
+        if (t < bestMs) {
+            bestMs = t;
+            best = c;
+        }
+    }
+    return best;
+}
+
 void PcgHandle::tuneSpmv() {
+    const auto t0 = std::chrono::steady_clock::now();
+    struct TuneClock {
+        std::chrono::steady_clock::time_point t0;
+        double* out;
+        ~TuneClock() { *out = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+    } clk{t0, &m_lastTuneMs};
     const int ncfg = numSpmvCfgs();
     int best = -1;
     float bestMs = 1e30f;
@@ -506,31 +556,7 @@ void PcgHandle::tuneSpmv() {
     } else {
         m_tuneMs.assign(ncfg, -1.f);
         check(cudaMemsetAsync(m_p.p, 0, sizeof(double) * m_n4, m_stream), "memset");
-        for (int c = 0; c < ncfg; ++c) {
-            const int grid = spmvGrid64(c);
-            if (grid <= 0) continue;
-            // one warm-up launch, then up to three timed ones; a configuration
-            // whose first timed launch is more than twice the best so far
-            // is not timed further (it keeps that one time)
-            float ms[3];
-            int timed = 0;
-            for (int rep = 0; rep < 4; ++rep) {
-                check(cudaEventRecord(m_ev0, m_stream), "event");
-                check(spmv64(c, grid, m_p.as<double>(), m_Ap.as<double>(), nullptr,
-                                          m_state.as<CgState>(), m_partials.as<double>(), kSpmvPlain, nullptr),
-                      "SpMV");
-                check(cudaEventRecord(m_ev1, m_stream), "event");
-                check(cudaEventSynchronize(m_ev1), "event");
-                if (rep > 0) check(cudaEventElapsedTime(&ms[timed++], m_ev0, m_ev1), "event");
-                if (rep == 1 && ms[0] > 2.f * bestMs) break;
-            }
-            std::sort(ms, ms + timed);
-            m_tuneMs[c] = ms[timed / 2];
-            if (ms[timed / 2] < bestMs) {
-                bestMs = ms[timed / 2];
-                best = c;
-            }
-        }
+        best = timeConfigs(false, m_tuneMs);
         if (best < 0) throw InternalError("no SpMV configuration can be launched on this device.");
     }
     m_spmvCfg = best;
@@ -578,31 +604,9 @@ void PcgHandle::tuneSpmv32() {
     int best = m_spmvCfg;
     m_tuneMs32.assign(ncfg, -1.f);
     if (m_forcedLanes == 0 && envInt("XJPCG_SPMV_CFG", -1) < 0) {
-        float bestMs = 1e30f;
         check(cudaMemsetAsync(m_p32.p, 0, vb32, m_stream), "memset");
-        for (int c = 0; c < ncfg; ++c) {
-            const int grid = spmvGrid32(c);
-            if (grid <= 0 || (isSell(c) && !ensureSell())) continue;
-            ensureValues32(c);
-            float ms[3];
-            int timed = 0;
-            for (int rep = 0; rep < 4; ++rep) {
-                check(cudaEventRecord(m_ev0, m_stream), "event");
-                check(spmv32(c, grid, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, m_state.as<CgState>(),
-                             m_partials.as<double>(), kSpmvPlain, nullptr),
-                      "SpMV fp32");
-                check(cudaEventRecord(m_ev1, m_stream), "event");
-                check(cudaEventSynchronize(m_ev1), "event");
-                if (rep > 0) check(cudaEventElapsedTime(&ms[timed++], m_ev0, m_ev1), "event");
-                if (rep == 1 && ms[0] > 2.f * bestMs) break;
-            }
-            std::sort(ms, ms + timed);
-            m_tuneMs32[c] = ms[timed / 2];
-            if (ms[timed / 2] < bestMs) {
-                bestMs = ms[timed / 2];
-                best = c;
-            }
-        }
+        const int b32 = timeConfigs(true, m_tuneMs32);
+        if (b32 >= 0) best = b32;
     }
     m_spmvCfg32 = best;
     m_spmvGrid32 = spmvGrid32(best);
@@ -873,18 +877,55 @@ Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
     ensureValues32(m_spmvCfg32);
     check(cudaMemsetAsync(m_Ap32.p, 0, vb32, m_stream), "memset");
     CgState* st = m_state.as<CgState>();
-    buildMixedGraph();
+    if (m_useGraph) buildMixedGraph();
     CgState cmd = {};
     cmd.tol = tol;
     cmd.maxIterP1 = maxIter + 1u;
-    cmd.useCond = 1;
-    cmd.condHandle = (uint64_t)m_condOuter;
-    cmd.relHandle = (uint64_t)m_condInner;
+    cmd.useCond = m_useGraph ? 1u : 0u;
+    cmd.condHandle = m_useGraph ? (uint64_t)m_condOuter : 0;
+    cmd.relHandle = m_useGraph ? (uint64_t)m_condInner : 0;
     const double delta = envDouble("XJPCG_RELIABLE_DELTA", 0.01);
     cmd.delta2 = delta * delta;
     check(cudaMemcpyAsync(st, &cmd, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
     check(cudaEventRecord(m_ev0, m_stream), "event");
-    check(cudaGraphLaunch(m_mixedExec, m_stream), "graph launch");
+    if (m_useGraph) {
+        check(cudaGraphLaunch(m_mixedExec, m_stream), "graph launch");
+    } else {
+        // Host-driven loop (profilers): the graph's kernels in batches of 16
+        // iterations; the refresh kernels skip themselves unless chosen.
+        const int n4 = (int)m_n4;
+        const int vg = vec_grid(n4, m_numSms);
+        double* part = m_partials.as<double>();
+        check(rel_init_launch(vg, m_stream, (int)m_n, n4, m_b.as<double>(), m_diag.as<double>(), m_x.as<double>(),
+                              m_d32.as<float>(), m_J32.as<float>(), m_r32.as<float>(), m_p32.as<float>(), st, part),
+              "mixed init");
+        uint64_t ran = 0;
+        for (;;) {
+            for (int u = 0; u < 16; ++u) {
+                check(spmv32(m_spmvCfg32, m_spmvGrid32, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, st, part,
+                             kSpmvCgDot, &st->done),
+                      "SpMV fp32");
+                check(rel_update_launch(vg, m_stream, n4, m_d32.as<float>(), m_r32.as<float>(), m_p32.as<float>(),
+                                        m_Ap32.as<float>(), m_J32.as<float>(), st, part),
+                      "mixed update");
+                check(rel_fold_launch(vg, m_stream, n4, m_x.as<double>(), m_d32.as<float>(), st), "fold");
+                check(spmv64(m_spmvCfg, m_spmvGrid, m_x.as<double>(), m_r.as<double>(), m_b.as<double>(), st, part,
+                             kSpmvResidual, &st->skipRefresh),
+                      "residual SpMV");
+                check(rel_restart_launch(vg, m_stream, n4, m_r.as<double>(), m_J32.as<float>(), m_r32.as<float>(),
+                                         st, part),
+                      "restart");
+                check(rel_pupdate_launch(vg, m_stream, n4, m_p32.as<float>(), m_r32.as<float>(), m_J32.as<float>(),
+                                         st),
+                      "p fp32");
+            }
+            ran += 16;
+            uint32_t done = 0;
+            check(cudaMemcpyAsync(&done, &st->done, sizeof(uint32_t), cudaMemcpyDeviceToHost, m_stream), "D2H");
+            check(cudaStreamSynchronize(m_stream), "sync");
+            if (done || ran > (uint64_t)maxIter + 1) break;
+        }
+    }
     check(cudaEventRecord(m_ev1, m_stream), "event");
     check(cudaMemcpyAsync(&m_lastState, st, sizeof(CgState), cudaMemcpyDeviceToHost, m_stream), "state download");
     check(cudaStreamSynchronize(m_stream), "sync");
@@ -1411,6 +1452,7 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->spmvLayout32 = layoutCode(c32);
     info->spmvCfg32 = m_spmvCfg32 >= 0 ? (uint32_t)m_spmvCfg32 : 0xffffffffu;
     info->spmvCfg = (uint32_t)m_spmvCfg;
+    info->tuneMs = m_lastTuneMs;
 }
 
 }  // namespace xjpcg

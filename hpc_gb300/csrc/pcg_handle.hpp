@@ -173,6 +173,7 @@ class PcgHandle {
     bool ensureSell();
     void ensureValues32(int cfg);
     void tuneSpmv32();
+    int timeConfigs(bool fp32, std::vector<float>& out);
     void refreshSellValues();
     cudaError_t spmv64(int cfg, int grid, const double* x, double* y, const double* b, CgState* st, double* part,
                        int mode, const uint32_t* done);
@@ -230,6 +231,7 @@ class PcgHandle {
     int m_spmvGrid32 = 0;
     uint64_t m_tuned32Gen = ~0ull;
     std::vector<float> m_tuneMs32;
+    double m_lastTuneMs = 0.0;  // wall time of the last FP64 tuning
 
     // vectors
     uint32_t m_vecN = 0, m_n4 = 0;

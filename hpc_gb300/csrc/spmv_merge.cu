@@ -306,7 +306,9 @@ namespace xjpcg {
 // the true-residual step of the refinement loop for the merge-path layout.
 template <typename VT>
 __global__ void __launch_bounds__(kMT) residual_finish_kernel(int n, const VT* __restrict__ b, VT* __restrict__ y,
-                                                              double* partials, CgState* state) {
+                                                              double* partials, CgState* state,
+                                                              const uint32_t* doneFlag) {
+    if (doneFlag && *(volatile const uint32_t*)doneFlag) return;
     double acc = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double r = (double)b[i] - (double)y[i];
@@ -320,10 +322,12 @@ __global__ void __launch_bounds__(kMT) residual_finish_kernel(int n, const VT* _
 }
 
 template <typename VT>
-cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, double* partials, CgState* state) {
+cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, double* partials, CgState* state,
+                                   const uint32_t* doneFlag) {
     const int grid = std::max(1, std::min((n + kMT - 1) / kMT, 152 * 8));
-    residual_finish_kernel<VT><<<grid, kMT, 0, st>>>(n, b, y, partials, state);
+    residual_finish_kernel<VT><<<grid, kMT, 0, st>>>(n, b, y, partials, state, doneFlag);
     return cudaGetLastError();
 }
-template cudaError_t residual_finish_launch<double>(cudaStream_t, int, const double*, double*, double*, CgState*);
+template cudaError_t residual_finish_launch<double>(cudaStream_t, int, const double*, double*, double*, CgState*,
+                                                    const uint32_t*);
 }  // namespace xjpcg

@@ -77,7 +77,8 @@ cudaError_t spmv_merge_launch(cudaStream_t st, int n, int nnz, const int* rowptr
                               const VT* x, VT* y, const int* tileRow, int* carryRow, void* carryVal, double* partials,
                               CgState* state, int mode, const uint32_t* doneFlag);
 template <typename VT>
-cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, double* partials, CgState* state);
+cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, double* partials, CgState* state,
+                                   const uint32_t* doneFlag);
 
 // ---- CG vector kernels (cg_kernels.cu) ----
 int vec_grid(int n4, int numSms);

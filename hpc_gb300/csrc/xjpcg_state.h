@@ -46,6 +46,8 @@ struct alignas(16) CgState {
     double rrMax;                  // mixed precision: largest r.r since the last refresh
     double delta2;                 // mixed precision: refresh when r.r < delta2 * rrMax
     uint64_t relHandle;            // mixed precision: conditional handle of the refresh
+    uint32_t skipRefresh;          // mixed precision: 1 = the refresh kernels of this iteration return at once
+    uint32_t pad0;
 };
 
 }  // namespace xjpcg

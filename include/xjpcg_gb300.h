@@ -44,6 +44,7 @@ typedef struct {
     uint32_t spmvCfg32;    /* index of the mixed solver's FP32 SpMV configuration (~0 until tuned) */
     uint32_t spmvLayout32; /* layout of that configuration, coded as spmvLayout */
     uint32_t reserved;
+    double tuneMs;         /* wall time of the last SpMV tuning (part of m_matProc) */
 } XJPCG_GbInfo_t;
 
 /* Per-system outcome of a batched solve. */

@@ -334,6 +334,32 @@ def test_host_loop_matches_graph_loop(gpu_lib):
     assert a.iters == b.iters and np.array_equal(a.x, b.x)
 
 
+@pytest.mark.parametrize("lanes", ["-3", "-2"])
+def test_mixed_host_loop_matches_graph_loop(gpu_lib, lanes):
+    # the mixed solver's host-driven loop (used under profilers) runs the
+    # graph's kernels with self-skipping refresh kernels: same iterates
+    s = W.diffusion27(14, seed=9)
+    os.environ["XJPCG_SPMV_LANES"] = lanes
+    try:
+        with X.JPCG() as h:
+            h.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
+            a = h.mixed_solve(s.b, s.diag, 20000, 1e-10)
+            ia = h.info()
+            assert ia.loopMode == 1
+        os.environ["XJPCG_HOST_LOOP"] = "1"
+        with X.JPCG() as h:
+            h.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
+            b = h.mixed_solve(s.b, s.diag, 20000, 1e-10)
+            ib = h.info()
+            assert ib.loopMode == 0
+    finally:
+        os.environ.pop("XJPCG_HOST_LOOP", None)
+        del os.environ["XJPCG_SPMV_LANES"]
+    assert a.status == X.SUCCESS and b.status == X.SUCCESS
+    assert a.iters == b.iters and ia.outerSweeps == ib.outerSweeps
+    assert a.res == b.res and np.array_equal(a.x, b.x)
+
+
 def test_zero_rhs_breakdown(handle):
     s = W.poisson7(8)
     rows, cols, vals = s.coo()
