@@ -50,9 +50,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the mixed-precision, batched and adjoint measurements")
-    ap.add_argument("--profile", choices=["spmv", "solve", "mixed"], default=None,
+    ap.add_argument("--profile", choices=["spmv", "solve", "mixed", "batched", "adjoint"], default=None,
                     help="profiling driver for ncu: set the matrix, then run --reps plain SpMVs "
-                         "(spmv), one resident fp64 solve (solve) or one mixed solve (mixed); no timing line")
+                         "(spmv), one resident fp64 solve (solve) or one mixed solve (mixed); or one batched "
+                         "solve of --systems systems (batched); or the adjoint solve and gradients on "
+                         "--nx^3 (adjoint); no timing line")
+    ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--workload", choices=["diffusion27", "zipf"], default="diffusion27",
                     help="matrix of --profile: diffusion27(--nx) or the 2M-row Zipf SPD system")
     ap.add_argument("--reps", type=int, default=4)
@@ -146,6 +149,26 @@ def run_profile(args):
     import torch
     import hpc_gb300 as X
     from hpc_gb300 import workloads as W
+    if args.profile == "batched":
+        systems = W.batched_stencils(count=args.systems, seed=3)
+        h = X.JPCG()
+        for prec in (0, 1):
+            st, _, res = h.batch_solve(systems, 20000, 1e-10, precision=prec)
+            print("batched precision=%d status=%d converged=%d" % (prec, st, int(np.sum(res["status"] == 0))),
+                  flush=True)
+        h.close()
+        return
+    if args.profile == "adjoint":
+        prob = W.adjoint_problem(args.nx, seed=4)
+        n = args.nx ** 3
+        s = W.assemble_edges(n, prob.edge_i, prob.edge_j, np.exp(prob.theta), W.ghost_diagonal7(prob.shape, prob.ghost))
+        h = X.JPCG()
+        r = h.csr_solve(n, s.rowptr, s.col, s.val, s.diag, prob.b, 20000, 1e-12)
+        st, lam, grad, it, res = h.adjoint(r.x - 0.5 * r.x, s.diag, 20000, 1e-12, grad_a=True)
+        g = h.edge_grad(prob.edge_i, prob.edge_j, np.exp(prob.theta))
+        print("adjoint forward=%d adjoint=%d status=%d" % (r.iters, it, st), flush=True)
+        h.close()
+        return
     sysm = W.diffusion27(args.nx) if args.workload == "diffusion27" else W.zipf_spd(2_000_000, seed=2)
     rows, cols, vals = sysm.coo()
     h = X.JPCG()

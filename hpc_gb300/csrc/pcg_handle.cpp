@@ -41,6 +41,7 @@ bool DevBuf::ensure(size_t b, uint64_t* generation) {
 PcgHandle::~PcgHandle() {
     if (m_exec) cudaGraphExecDestroy(m_exec);
     if (m_mixedExec) cudaGraphExecDestroy(m_mixedExec);
+    if (m_batchExec) cudaGraphExecDestroy(m_batchExec);
     if (m_ev0) cudaEventDestroy(m_ev0);
     if (m_ev1) cudaEventDestroy(m_ev1);
     if (m_stream) cudaStreamDestroy(m_stream);
@@ -385,12 +386,13 @@ int PcgHandle::spmvGrid32(int cfg) {
     if (isSorted(cfg))
         return ensureSorted() ? sellsort_grid<float>(cfg - sortedCfg0(), (int)m_n, m_ssLong, m_numSms) : 0;
     if (!isSell(cfg)) return spmv_grid<float>(cfg, (int)m_n, m_numSms);
-    if (isSellNarrow(cfg) && !m_sellNarrow) return 0;
+    if (!ensureSell() || (isSellNarrow(cfg) && !m_sellNarrow)) return 0;
     return sell_grid<float>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
 }
 
 cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, const double* b, CgState* st,
                               double* part, int mode, const uint32_t* done) {
+    if (isMerge(cfg) && !m_mergeTilesValid) return cudaErrorInvalidValue;
     if (isMerge(cfg)) {
         const int m = mode == kSpmvResidual ? kSpmvPlain : mode;
         cudaError_t e = spmv_merge_launch<double>(m_stream, (int)m_n, (int)m_nnz, m_rowptr.as<int>(), m_col.as<int>(),
@@ -400,6 +402,10 @@ cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, con
         if (e != cudaSuccess || mode != kSpmvResidual) return e;
         return residual_finish_launch<double>(m_stream, (int)m_n, b, y, part, st, done);
     }
+    // a layout whose copy was not built (or was rejected) is never launched
+    if ((isSorted(cfg) && m_ssState != 1) || (isSell(cfg) && m_sellState != 1) ||
+        (isSellNarrow(cfg) && !m_sellNarrow))
+        return cudaErrorInvalidValue;
     if (isSorted(cfg))
         return spmv_sellsort_launch<double>(cfg - sortedCfg0(), grid, m_stream, (int)m_n, m_ssLong,
                                             m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), m_ssCol.as<int>(),
@@ -415,11 +421,15 @@ cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, con
 
 cudaError_t PcgHandle::spmv32(int cfg, int grid, const float* x, float* y, const float* b, CgState* st,
                               double* part, int mode, const uint32_t* done) {
+    if (isMerge(cfg) && (!m_mergeTilesValid || !m_val32Valid)) return cudaErrorInvalidValue;
     if (isMerge(cfg))  // the fp32 inner loop only uses the kCgDot mode
         return spmv_merge_launch<float>(m_stream, (int)m_n, (int)m_nnz, m_rowptr.as<int>(), m_col.as<int>(),
                                         m_val32.as<float>(), x, y, m_mergeTile.as<int>(), m_mergeRow.as<int>(),
                                         m_mergeVal.p,
                                         m_mergePart.as<double>(), st, mode, done);
+    if ((isSorted(cfg) && (m_ssState != 1 || !m_ss32Valid)) || (isSell(cfg) && (m_sellState != 1 || !m_sell32Valid)) ||
+        (isSellNarrow(cfg) && !m_sellNarrow) || !m_val32Valid)
+        return cudaErrorInvalidValue;
     if (isSorted(cfg))
         return spmv_sellsort_launch<float>(cfg - sortedCfg0(), grid, m_stream, (int)m_n, m_ssLong,
                                            m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), m_ssCol.as<int>(),
@@ -574,14 +584,14 @@ void PcgHandle::ensureValues32(int cfg) {
         check(convert_f64_to_f32(m_stream, (int64_t)nnzPad, m_val.as<double>(), m_val32.as<float>()), "fp32 values");
         m_val32Valid = true;
     }
-    if (isSorted(cfg) && !m_ss32Valid) {
+    if (isSorted(cfg) && m_ssState == 1 && !m_ss32Valid) {
         alloc(m_ssVal32, sizeof(float) * ((size_t)m_ssTotal + 32), "sorted sliced fp32 values");
         check(sellsort_fill<float>(m_stream, (int)m_n, m_ssLong, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
                                    m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), nullptr, m_ssVal32.as<float>()),
               "sorted sliced fp32 fill");
         m_ss32Valid = true;
     }
-    if (isSell(cfg) && !m_sell32Valid) {
+    if (isSell(cfg) && m_sellState == 1 && !m_sell32Valid) {
         alloc(m_sellVal32, sizeof(float) * ((size_t)m_sellTotal + 32), "sliced fp32 values");
         check(sell_fill<float>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
                                m_sliceOff.as<int>(), nullptr, m_sellVal32.as<float>()),
@@ -1331,7 +1341,33 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
             }
         m_batchKey = key;
     }
-    runOnce(m_batchCfg, m_batchSmemRows, &m_batchMs);
+    // The production launch is a CUDA graph (queue reset + persistent
+    // kernel), instantiated once per shape and buffer set.
+    const uint64_t gkey = mixKey(mixKey(mixKey(key, (uint64_t)m_batchCfg), (uint64_t)m_batchSmemRows), m_generation);
+    if (!m_batchExec || m_batchExecKey != gkey) {
+        if (m_batchExec) {
+            cudaGraphExecDestroy(m_batchExec);
+            m_batchExec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        check(cudaStreamBeginCapture(m_stream, cudaStreamCaptureModeThreadLocal), "capture");
+        int grid = 0;
+        cudaError_t e1 = cudaMemsetAsync(m_bQueue.p, 0, 16, m_stream);
+        cudaError_t e2 = e1 == cudaSuccess ? batch_launch(m_batchCfg, mixed, m_numSms, m_batchSmemRows, m_stream, L, &grid)
+                                           : e1;
+        cudaError_t e3 = cudaStreamEndCapture(m_stream, &g);
+        check(e2, "batched kernel capture");
+        check(e3, "capture end");
+        check(cudaGraphInstantiate(&m_batchExec, g, 0), "graph instantiate");
+        cudaGraphDestroy(g);
+        m_batchGrid = grid;
+        m_batchExecKey = gkey;
+    }
+    check(cudaEventRecord(m_ev0, m_stream), "event");
+    check(cudaGraphLaunch(m_batchExec, m_stream), "graph launch");
+    check(cudaEventRecord(m_ev1, m_stream), "event");
+    check(cudaEventSynchronize(m_ev1), "event");
+    check(cudaEventElapsedTime(&m_batchMs, m_ev0, m_ev1), "event");
     std::vector<BatchResult> hr(nsys);
     check(cudaMemcpyAsync(results ? (void*)results : (void*)hr.data(), m_bRes.p, sizeof(BatchResult) * nsys,
                           cudaMemcpyDeviceToHost, m_stream),

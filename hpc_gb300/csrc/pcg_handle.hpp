@@ -258,6 +258,8 @@ class PcgHandle {
     uint64_t m_batchKey = 0;
     float m_batchMs = 0.f;
     std::vector<float> m_batchTuneMs;
+    cudaGraphExec_t m_batchExec = nullptr;  // queue reset + persistent kernel
+    uint64_t m_batchExecKey = 0;
 
     // graph
     cudaGraphExec_t m_exec = nullptr;
