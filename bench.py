@@ -50,11 +50,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the mixed-precision, batched and adjoint measurements")
-    ap.add_argument("--profile", choices=["spmv", "solve", "mixed", "batched", "adjoint"], default=None,
+    ap.add_argument("--profile", choices=["spmv", "solve", "mixed", "batched", "adjoint", "export"], default=None,
                     help="profiling driver for ncu: set the matrix, then run --reps plain SpMVs "
                          "(spmv), one resident fp64 solve (solve) or one mixed solve (mixed); or one batched "
                          "solve of --systems systems (batched); or the adjoint solve and gradients on "
-                         "--nx^3 (adjoint); no timing line")
+                         "--nx^3 (adjoint); or the signature export of the matrix (export); no timing line")
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--workload", choices=["diffusion27", "zipf"], default="diffusion27",
                     help="matrix of --profile: diffusion27(--nx) or the 2M-row Zipf SPD system")
@@ -178,7 +178,11 @@ def run_profile(args):
           flush=True)
     d_b = torch.from_numpy(sysm.b).cuda()
     d_y = torch.zeros_like(d_b)
-    if args.profile == "spmv":
+    if args.profile == "export":
+        for _ in range(args.reps):
+            files = h.export_signature()
+        print("export bytes=%d" % sum(len(v) for v in files.values()), flush=True)
+    elif args.profile == "spmv":
         for _ in range(args.reps):
             h.spmv(d_b.data_ptr(), d_y.data_ptr(), on_device=True)
     elif args.profile == "solve":

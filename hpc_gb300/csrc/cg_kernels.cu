@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_init_kernel(int n, int n4, con
     }
 }
 
-__global__ void __launch_bounds__(kVecThreads) cg_update_kernel(int n4, double* __restrict__ x, double* __restrict__ r,
+__global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, double* __restrict__ x, double* __restrict__ r,
                                                                 const double* __restrict__ p,
                                                                 const double* __restrict__ Ap,
                                                                 const double* __restrict__ J, CgState* state,
@@ -106,7 +106,37 @@ __global__ void __launch_bounds__(kVecThreads) cg_update_kernel(int n4, double* 
     const double2* p2 = reinterpret_cast<const double2*>(p);
     const double2* a2 = reinterpret_cast<const double2*>(Ap);
     const double2* j2 = reinterpret_cast<const double2*>(J);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+    // Two elements per step, all ten loads issued before any arithmetic,
+    // so each thread keeps 160 bytes in flight.
+    const int stride = gridDim.x * blockDim.x;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + stride < n2; i += 2 * stride) {
+        double2 xv[2], rv[2], pv[2], av[2], jv[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int e = i + u * stride;
+            xv[u] = x2[e];
+            rv[u] = r2[e];
+            pv[u] = p2[e];
+            av[u] = __ldcs(&a2[e]);
+            jv[u] = j2[e];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            xv[u].x = fma(alpha, pv[u].x, xv[u].x);
+            xv[u].y = fma(alpha, pv[u].y, xv[u].y);
+            rv[u].x = fma(-alpha, av[u].x, rv[u].x);
+            rv[u].y = fma(-alpha, av[u].y, rv[u].y);
+            const double z0 = rv[u].x * jv[u].x, z1 = rv[u].y * jv[u].y;
+            rr = fma(rv[u].x, rv[u].x, rr);
+            rr = fma(rv[u].y, rv[u].y, rr);
+            rz = fma(rv[u].x, z0, rz);
+            rz = fma(rv[u].y, z1, rz);
+            x2[i + u * stride] = xv[u];
+            r2[i + u * stride] = rv[u];
+        }
+    }
+    for (; i < n2; i += stride) {
         double2 xv = x2[i], rv = r2[i];
         const double2 pv = p2[i], av = __ldcs(&a2[i]), jv = j2[i];
         xv.x = fma(alpha, pv.x, xv.x);
@@ -163,6 +193,15 @@ __global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double*
         pv.y = fma(beta, pv.y, rv.y * jv.y);
         p2[i] = pv;
     }
+}
+
+// The update kernel holds two elements per step (48 registers): one wave of
+// 5 CTAs per SM.
+int update_grid(int n4, int numSms) {
+    int need = (n4 / 2 + kVecThreads - 1) / kVecThreads;
+    int cap = numSms * 5;
+    if (need < 1) need = 1;
+    return need < cap ? need : cap;
 }
 
 int vec_grid(int n4, int numSms) {

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kMxThreads) rel_init_kernel(int n, int n4, con
     }
 }
 
-__global__ void __launch_bounds__(kMxThreads) rel_update_kernel(int n4, float* __restrict__ d, float* __restrict__ r,
+__global__ void __launch_bounds__(kMxThreads, 5) rel_update_kernel(int n4, float* __restrict__ d, float* __restrict__ r,
                                                                 const float* __restrict__ p,
                                                                 const float* __restrict__ Ap,
                                                                 const float* __restrict__ J, CgState* st,
@@ -100,7 +100,43 @@ __global__ void __launch_bounds__(kMxThreads) rel_update_kernel(int n4, float* _
     const float4* p4 = reinterpret_cast<const float4*>(p);
     const float4* a4 = reinterpret_cast<const float4*>(Ap);
     const float4* j4 = reinterpret_cast<const float4*>(J);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4q; i += gridDim.x * blockDim.x) {
+    // Two float4 per step, all ten loads issued before any arithmetic.
+    const int stride = gridDim.x * blockDim.x;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + stride < n4q; i += 2 * stride) {
+        float4 dv[2], rv[2], pv[2], av[2], jv[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int e = i + u * stride;
+            dv[u] = d4[e];
+            rv[u] = r4[e];
+            pv[u] = p4[e];
+            av[u] = __ldcs(&a4[e]);
+            jv[u] = j4[e];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            dv[u].x = fmaf(alpha, pv[u].x, dv[u].x);
+            dv[u].y = fmaf(alpha, pv[u].y, dv[u].y);
+            dv[u].z = fmaf(alpha, pv[u].z, dv[u].z);
+            dv[u].w = fmaf(alpha, pv[u].w, dv[u].w);
+            rv[u].x = fmaf(-alpha, av[u].x, rv[u].x);
+            rv[u].y = fmaf(-alpha, av[u].y, rv[u].y);
+            rv[u].z = fmaf(-alpha, av[u].z, rv[u].z);
+            rv[u].w = fmaf(-alpha, av[u].w, rv[u].w);
+            rr = fmaf(rv[u].x, rv[u].x, rr);
+            rr = fmaf(rv[u].y, rv[u].y, rr);
+            rr = fmaf(rv[u].z, rv[u].z, rr);
+            rr = fmaf(rv[u].w, rv[u].w, rr);
+            rz = fmaf(rv[u].x, rv[u].x * jv[u].x, rz);
+            rz = fmaf(rv[u].y, rv[u].y * jv[u].y, rz);
+            rz = fmaf(rv[u].z, rv[u].z * jv[u].z, rz);
+            rz = fmaf(rv[u].w, rv[u].w * jv[u].w, rz);
+            d4[i + u * stride] = dv[u];
+            r4[i + u * stride] = rv[u];
+        }
+    }
+    for (; i < n4q; i += stride) {
         float4 dv = d4[i], rv = r4[i];
         const float4 pv = p4[i], av = __ldcs(&a4[i]), jv = j4[i];
         dv.x = fmaf(alpha, pv.x, dv.x);
