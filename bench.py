@@ -286,14 +286,22 @@ def batched_measure(X, count=4096):
     systems = W.batched_stencils(count=count, seed=3)
     h = X.JPCG()
     out = {"systems": count, "rows": int(sum(s.n for s in systems)), "nnz": int(sum(s.nnz for s in systems))}
+    import oracle
+    # error against a tight FP64 oracle solve on a sample of the systems
+    sample = list(range(0, count, max(1, count // 16)))[:16]
+    tight = {i: oracle.jpcg(systems[i].rowptr, systems[i].col, systems[i].val, systems[i].diag, systems[i].b,
+                            200000, 1e-14)["x"] for i in sample}
     for prec, key in ((0, "fp64"), (1, "mixed")):
         st, _, res = h.batch_solve(systems, 20000, 1e-10, precision=prec)  # includes tuning on first use
-        st, _, res = h.batch_solve(systems, 20000, 1e-10, precision=prec)
+        st, xs, res = h.batch_solve(systems, 20000, 1e-10, precision=prec)
         inf = h.info()
+        err = max(float(np.linalg.norm(xs[i] - tight[i]) / np.linalg.norm(tight[i])) for i in sample)
         out[key] = {"status": st, "device_ms": inf.batchMs, "systems_per_s": count / (inf.batchMs / 1e3),
                     "converged": int(np.sum((res["status"] == 0) & (res["res"] <= 1e-10))),
                     "iters_total": int(res["itersRun"].sum()), "threads": inf.batchThreads,
-                    "lanes": inf.batchLanes, "smem_rows": inf.batchSmemRows, "grid": inf.batchGrid}
+                    "lanes": inf.batchLanes, "smem_rows": inf.batchSmemRows, "grid": inf.batchGrid,
+                    "max_err_vs_oracle_sample": err,
+                    "oracle": "oracle JPCG to 1e-14 (FP64, CPU) on %d sampled systems" % len(sample)}
     h.close()
     return out
 
@@ -476,8 +484,15 @@ def run_gb300(args):
         import oracle
         S = args.cpu_sample_iters
         per_iter, dt = cpu_sample(sysm, k_iters, S)
+        xs = np.asarray(sysm.b)
+        oracle.spmv(sysm.rowptr, sysm.col, sysm.val, xs)
+        t0 = time.perf_counter()
+        for _ in range(5):
+            oracle.spmv(sysm.rowptr, sysm.col, sysm.val, xs)
+        spmv_cpu_s = (time.perf_counter() - t0) / 5
         cpu = {"value": 1.0 / (per_iter * k_iters), "unit": "solves/s", "cores": oracle.max_threads(),
-               "kind": "port",
+               "kind": "port", "spmv_gbs": spmv_bytes(n, nnz) / spmv_cpu_s / 1e9,
+               "spmv_note": "oracle CSR SpMV (12 B per entry), all host cores, 5 launches",
                "sample": "%d oracle JPCG iterations on the full 160^3 system (%.1f s), scaled to the %d "
                          "iterations of the GPU solve" % (S, dt, k_iters)}
 

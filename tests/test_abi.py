@@ -72,3 +72,22 @@ def test_struct_layouts():
     assert X.RECORD_DTYPE.itemsize == 64
     assert list(X.RECORD_DTYPE.names) == ["id", "iter", "vecSize", "maxIter", "tols", "res", "rz", "alpha",
                                           "beta", "clock"]
+
+
+def test_ctypes_mirrors_match_the_header(tmp_path):
+    """The binding's ctypes structs have the C header's sizes and offsets."""
+    import subprocess
+    exe = str(tmp_path / "abi_layout")
+    subprocess.run(["gcc", "-std=c99", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c", "abi_layout.c"), "-o", exe], check=True)
+    out = dict(line.split("=") for line in subprocess.run([exe], capture_output=True, text=True,
+                                                         check=True).stdout.split())
+    mirrors = {"XJPCG_GbInfo_t": X.GbInfo, "XJPCG_GbSignature_t": X.GbSignature}
+    for cname, py in mirrors.items():
+        assert int(out[cname]) == C.sizeof(py), cname
+        for key, val in out.items():
+            if key.startswith(cname + "."):
+                assert int(val) == getattr(py, key.split(".")[1]).offset, key
+    assert int(out["XJPCG_GbBatchResult_t"]) == X.BATCH_RESULT_DTYPE.itemsize
+    assert int(out["XJPCG_GbBatchResult_t.res"]) == X.BATCH_RESULT_DTYPE.fields["res"][1]
+    assert int(out["XJPCG_Metric_t"]) == C.sizeof(X.Metric)
