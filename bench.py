@@ -205,7 +205,9 @@ LAYOUTS = {0: ("csr_staged", "spmv_ws_kernel (TMA-staged CSR fp64 SpMV)", 4),
            2: ("merge_path", "spmv_merge_kernel (merge-path CSR fp64 SpMV)", 4),
            3: ("sliced16", "spmv_sell_kernel<double,U,int16_t> (SELL-32 fp64 SpMV, int16 column offsets)", 2),
            4: ("sliced_sorted", "spmv_sellsort_kernel<double,U> (length-sorted SELL-32 fp64 SpMV, long rows per warp)",
-               4)}
+               4),
+           5: ("sliced_shared", "spmv_sellpat_kernel<double,U> (SELL-32 fp64 SpMV, column offsets shared per slice)",
+               0)}
 
 
 def spmv_bytes(n, nnz, col_bytes=4):

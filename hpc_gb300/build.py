@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
            "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
-SOURCES = ["spmv_kernels.cu", "spmv_sellsort.cu", "spmv_merge.cu", "cg_kernels.cu", "mixed_kernels.cu", "convert_kernels.cu",
+SOURCES = ["spmv_kernels.cu", "spmv_sellpat.cu", "spmv_sellsort.cu", "spmv_merge.cu", "cg_kernels.cu", "mixed_kernels.cu", "convert_kernels.cu",
            "spmv_noalloc.cu", "batched_kernels.cu", "adjoint_kernels.cu", "signature_kernels.cu", "signature_export.cu", "pcg_handle.cpp", "pcg_api.cpp"]
 HEADERS = ["xjpcg_device.cuh", "xjpcg_state.h", "xjpcg_internal.hpp", "pcg_handle.hpp"]
 

@@ -257,6 +257,8 @@ void PcgHandle::finishMatrix() {
     m_sell32Valid = false;
     m_ssState = 0;
     m_ss32Valid = false;
+    m_psState = 0;
+    m_ps32Valid = false;
     m_mergeTilesValid = false;
     ++m_structGen;
     check(cudaStreamSynchronize(m_stream), "sync");
@@ -279,6 +281,13 @@ void PcgHandle::refreshSellValues() {
         check(sell_fill<double>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
                                 m_sliceOff.as<int>(), nullptr, m_sellVal.as<double>()),
               "sliced fill");
+    m_ps32Valid = false;
+    if (m_psState == 1)
+        check(sellpat_fill<double>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                                   m_psSliceOff.as<int>(), m_psPatLen.as<int>(), m_psPatNew.as<int>(),
+                                   m_psPatIdx.as<int>(), m_psPatOff.as<int>(), m_psGenOff.as<int>(), m_psVal.as<double>(),
+                                   nullptr, nullptr, false),
+              "shared-offset fill");
     if (m_ssState == 1)
         check(sellsort_fill<double>(m_stream, (int)m_n, m_ssLong, m_rowptr.as<int>(), m_col.as<int>(),
                                     m_val.as<double>(), m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), nullptr,
@@ -291,7 +300,9 @@ void PcgHandle::refreshSellValues() {
 // merge-path kernel.
 int PcgHandle::numSpmvCfgs() const { return mergeCfg() + 1; }
 
-int PcgHandle::sortedCfg0() const { return spmv_num_configs() + sell_num_configs(); }
+int PcgHandle::patCfg0() const { return spmv_num_configs() + sell_num_configs(); }
+
+int PcgHandle::sortedCfg0() const { return patCfg0() + sellpat_num_configs(); }
 
 int PcgHandle::mergeCfg() const { return sortedCfg0() + sellsort_num_configs(); }
 
@@ -303,13 +314,58 @@ bool PcgHandle::isSellNarrow(int cfg) const { return isSell(cfg) && sell_config_
 
 bool PcgHandle::isSorted(int cfg) const { return cfg >= sortedCfg0() && cfg < mergeCfg(); }
 
+bool PcgHandle::isPat(int cfg) const { return cfg >= patCfg0() && cfg < sortedCfg0(); }
+
 bool PcgHandle::isMerge(int cfg) const { return cfg == mergeCfg(); }
 
 uint32_t PcgHandle::layoutCode(int cfg) const {
     if (isMerge(cfg)) return 2u;
+    if (isPat(cfg)) return 5u;
     if (isSorted(cfg)) return 4u;
     if (isSellNarrow(cfg)) return 3u;
     return isSell(cfg) ? 1u : 0u;
+}
+
+// Builds (once per matrix) the sliced copy with slice-shared column offsets.
+// Offered for matrices the plain sliced layout suits.
+bool PcgHandle::ensurePat() {
+    if (m_psState == 1) return true;
+    if (m_psState == 2) return false;
+    if (!ensureSell()) {
+        m_psState = 2;
+        return false;
+    }
+    const int n = (int)m_n;
+    const int nslices = (n + 31) / 32;
+    const size_t sb = sizeof(int) * ((size_t)nslices + 1);
+    for (DevBuf* b : {&m_psSliceOff, &m_psPatLen, &m_psPatNew, &m_psPatIdx, &m_psGenOff}) alloc(*b, sb, "shared-offset slices");
+    alloc(m_psPatOff, sb, "shared-offset patterns");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count(std::max(nslices, n) + 1) + 16), "scan scratch");
+    int64_t tot[3] = {0, 0, 0};
+    check(sellpat_plan(m_stream, n, m_rowptr.as<int>(), m_col.as<int>(), m_psSliceOff.as<int>(), m_psPatLen.as<int>(),
+                       m_psPatNew.as<int>(), m_psPatIdx.as<int>(), m_psPatOff.as<int>(), m_psGenOff.as<int>(), nullptr,
+                       m_blockSums.as<int>(), tot),
+          "shared-offset layout");
+    if (tot[0] > 0x7fffff00ll) {
+        m_psState = 2;
+        return false;
+    }
+    int64_t patTotal = 0;
+    check(sellpat_index(m_stream, n, m_psPatLen.as<int>(), m_psPatNew.as<int>(), m_psPatIdx.as<int>(), (int)tot[2],
+                        m_psPatOff.as<int>(), m_blockSums.as<int>(), &patTotal),
+          "shared-offset patterns");
+    alloc(m_psPat, sizeof(int) * ((size_t)patTotal + 32), "shared offsets");
+    alloc(m_psGcol, sizeof(int) * ((size_t)tot[1] + 32), "shared-offset general columns");
+    alloc(m_psVal, sizeof(double) * ((size_t)tot[0] + 32), "shared-offset values");
+    check(sellpat_fill<double>(m_stream, n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                               m_psSliceOff.as<int>(), m_psPatLen.as<int>(), m_psPatNew.as<int>(), m_psPatIdx.as<int>(),
+                               m_psPatOff.as<int>(), m_psGenOff.as<int>(), m_psVal.as<double>(), m_psPat.as<int>(),
+                               m_psGcol.as<int>(), true),
+          "shared-offset fill");
+    m_psTotal = tot[0];
+    m_psState = 1;
+    m_ps32Valid = false;
+    return true;
 }
 
 // Builds (once per matrix) the length-sorted sliced copy.  Only offered when
@@ -373,6 +429,7 @@ int PcgHandle::spmvGrid64(int cfg) {
     }
     if (isSorted(cfg))
         return ensureSorted() ? sellsort_grid<double>(cfg - sortedCfg0(), (int)m_n, m_ssLong, m_numSms) : 0;
+    if (isPat(cfg)) return ensurePat() ? sellpat_grid<double>(cfg - patCfg0(), (int)m_n, m_numSms) : 0;
     if (!isSell(cfg)) return spmv_grid<double>(cfg, (int)m_n, m_numSms);
     if (!ensureSell() || (isSellNarrow(cfg) && !m_sellNarrow)) return 0;
     return sell_grid<double>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
@@ -385,6 +442,7 @@ int PcgHandle::spmvGrid32(int cfg) {
     }
     if (isSorted(cfg))
         return ensureSorted() ? sellsort_grid<float>(cfg - sortedCfg0(), (int)m_n, m_ssLong, m_numSms) : 0;
+    if (isPat(cfg)) return ensurePat() ? sellpat_grid<float>(cfg - patCfg0(), (int)m_n, m_numSms) : 0;
     if (!isSell(cfg)) return spmv_grid<float>(cfg, (int)m_n, m_numSms);
     if (!ensureSell() || (isSellNarrow(cfg) && !m_sellNarrow)) return 0;
     return sell_grid<float>(cfg - spmv_num_configs(), (int)m_n, m_numSms);
@@ -404,8 +462,13 @@ cudaError_t PcgHandle::spmv64(int cfg, int grid, const double* x, double* y, con
     }
     // a layout whose copy was not built (or was rejected) is never launched
     if ((isSorted(cfg) && m_ssState != 1) || (isSell(cfg) && m_sellState != 1) ||
-        (isSellNarrow(cfg) && !m_sellNarrow))
+        (isSellNarrow(cfg) && !m_sellNarrow) || (isPat(cfg) && m_psState != 1))
         return cudaErrorInvalidValue;
+    if (isPat(cfg))
+        return spmv_sellpat_launch<double>(cfg - patCfg0(), grid, m_stream, (int)m_n, m_psSliceOff.as<int>(),
+                                           m_psPatLen.as<int>(), m_psPatIdx.as<int>(), m_psPatOff.as<int>(),
+                                           m_psGenOff.as<int>(), m_psPat.as<int>(), m_psGcol.as<int>(),
+                                           m_psVal.as<double>(), x, y, b, st, part, mode, done);
     if (isSorted(cfg))
         return spmv_sellsort_launch<double>(cfg - sortedCfg0(), grid, m_stream, (int)m_n, m_ssLong,
                                             m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), m_ssCol.as<int>(),
@@ -428,8 +491,13 @@ cudaError_t PcgHandle::spmv32(int cfg, int grid, const float* x, float* y, const
                                         m_mergeVal.p,
                                         m_mergePart.as<double>(), st, mode, done);
     if ((isSorted(cfg) && (m_ssState != 1 || !m_ss32Valid)) || (isSell(cfg) && (m_sellState != 1 || !m_sell32Valid)) ||
-        (isSellNarrow(cfg) && !m_sellNarrow) || !m_val32Valid)
+        (isSellNarrow(cfg) && !m_sellNarrow) || (isPat(cfg) && (m_psState != 1 || !m_ps32Valid)) || !m_val32Valid)
         return cudaErrorInvalidValue;
+    if (isPat(cfg))
+        return spmv_sellpat_launch<float>(cfg - patCfg0(), grid, m_stream, (int)m_n, m_psSliceOff.as<int>(),
+                                          m_psPatLen.as<int>(), m_psPatIdx.as<int>(), m_psPatOff.as<int>(),
+                                          m_psGenOff.as<int>(), m_psPat.as<int>(), m_psGcol.as<int>(),
+                                          m_psVal32.as<float>(), x, y, b, st, part, mode, done);
     if (isSorted(cfg))
         return spmv_sellsort_launch<float>(cfg - sortedCfg0(), grid, m_stream, (int)m_n, m_ssLong,
                                            m_ssSorted.as<int>(), m_ssSliceOff.as<int>(), m_ssCol.as<int>(),
@@ -549,6 +617,9 @@ void PcgHandle::tuneSpmv() {
         best = forcedCfg;
     } else if (m_forcedLanes == -2) {
         best = mergeCfg();
+    } else if (m_forcedLanes == -5) {
+        if (!ensurePat()) throw InvalidValue("the shared-offset sliced SpMV layout is not offered for this matrix.");
+        best = patCfg0() + 1;  // unroll 8
     } else if (m_forcedLanes == -4) {
         if (!ensureSorted())
             throw InvalidValue("the length-sorted sliced SpMV layout is not offered for this matrix.");
@@ -584,6 +655,15 @@ void PcgHandle::ensureValues32(int cfg) {
         alloc(m_val32, sizeof(float) * nnzPad, "fp32 values");
         check(convert_f64_to_f32(m_stream, (int64_t)nnzPad, m_val.as<double>(), m_val32.as<float>()), "fp32 values");
         m_val32Valid = true;
+    }
+    if (isPat(cfg) && m_psState == 1 && !m_ps32Valid) {
+        alloc(m_psVal32, sizeof(float) * ((size_t)m_psTotal + 32), "shared-offset fp32 values");
+        check(sellpat_fill<float>(m_stream, (int)m_n, m_rowptr.as<int>(), m_col.as<int>(), m_val.as<double>(),
+                                  m_psSliceOff.as<int>(), m_psPatLen.as<int>(), m_psPatNew.as<int>(),
+                                  m_psPatIdx.as<int>(), m_psPatOff.as<int>(), m_psGenOff.as<int>(), m_psVal32.as<float>(),
+                                  nullptr, nullptr, false),
+              "shared-offset fp32 fill");
+        m_ps32Valid = true;
     }
     if (isSorted(cfg) && m_ssState == 1 && !m_ss32Valid) {
         alloc(m_ssVal32, sizeof(float) * ((size_t)m_ssTotal + 32), "sorted sliced fp32 values");
@@ -1439,6 +1519,12 @@ int PcgHandle::tuning(float* ms, int* shape, int cap) const {
             shape[4 * c] = 0;
             shape[4 * c + 1] = 256;
             shape[4 * c + 2] = merge_items_per_thread();
+            shape[4 * c + 3] = 0;
+        } else if (isPat(c)) {
+            // shared-offset sliced layout: (1, 2, unroll, 0)
+            shape[4 * c] = 1;
+            shape[4 * c + 1] = 2;
+            shape[4 * c + 2] = sellpat_config_unroll(c - patCfg0());
             shape[4 * c + 3] = 0;
         } else if (isSorted(c)) {
             // length-sorted sliced layout: (1, 1, unroll, 32)

@@ -162,6 +162,9 @@ class PcgHandle {
     bool isSell(int cfg) const;
     bool isSellNarrow(int cfg) const;
     bool isSorted(int cfg) const;
+    bool isPat(int cfg) const;
+    int patCfg0() const;
+    bool ensurePat();
     int sortedCfg0() const;
     int mergeCfg() const;
     uint32_t layoutCode(int cfg) const;
@@ -209,6 +212,12 @@ class PcgHandle {
     DevBuf m_sellCol16;          // int16 column offsets (when the matrix is narrow enough)
     bool m_sellNarrow = false;
     double m_sellPadRatio = 0.0;  // stored / real entries of the sliced copy
+    // sliced copy with slice-shared column offsets (structured grids)
+    DevBuf m_psSliceOff, m_psPatLen, m_psPatNew, m_psPatIdx, m_psPatOff, m_psGenOff, m_psPat, m_psGcol, m_psVal,
+        m_psVal32;
+    int m_psState = 0;  // 0 not built, 1 built, 2 not offered
+    int64_t m_psTotal = 0;
+    bool m_ps32Valid = false;
     // length-sorted sliced copy (irregular rows)
     DevBuf m_ssSorted, m_ssHist, m_ssStart, m_ssSliceOff, m_ssCol, m_ssVal, m_ssVal32;
     int m_ssState = 0;  // 0 not built, 1 built, 2 not offered

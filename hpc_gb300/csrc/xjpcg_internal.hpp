@@ -43,6 +43,29 @@ cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const in
                              const int16_t* scol16, const VT* sval, const VT* x, VT* y, const VT* b, CgState* state,
                              double* partials, int mode, const uint32_t* doneFlag);
 
+// ---- sliced SpMV with slice-shared column offsets (spmv_sellpat.cu) ----
+int sellpat_num_configs();
+int sellpat_config_unroll(int cfg);
+// All per-slice arrays hold nslices + 1 ints.  totals = {stored values,
+// general-slice columns, stored patterns}.
+cudaError_t sellpat_plan(cudaStream_t st, int n, const int* rowptr, const int* col, int* sliceOff, int* patLen,
+                         int* patNew, int* patIdx, int* patOff, int* genOff, int* scratch, int* blockSums,
+                         int64_t* totals);
+// patOff: nPatterns + 1 ints; *patTotal = stored pattern entries.
+cudaError_t sellpat_index(cudaStream_t st, int n, const int* patLen, const int* patNew, int* patIdx, int nPatterns,
+                          int* patOff, int* blockSums, int64_t* patTotal);
+template <typename VT>
+cudaError_t sellpat_fill(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val,
+                         const int* sliceOff, const int* patLen, const int* patNew, const int* patIdx,
+                         const int* patOff, const int* genOff, VT* sval, int* pat, int* gcol, bool writeIndex);
+template <typename VT>
+int sellpat_grid(int cfg, int n, int numSms);
+template <typename VT>
+cudaError_t spmv_sellpat_launch(int cfg, int grid, cudaStream_t st, int n, const int* sliceOff, const int* patLen,
+                                const int* patIdx, const int* patOff, const int* genOff, const int* pat,
+                                const int* gcol, const VT* sval, const VT* x, VT* y, const VT* b, CgState* state,
+                                double* partials, int mode, const uint32_t* doneFlag);
+
 // ---- length-sorted sliced SpMV (spmv_sellsort.cu) ----
 int sellsort_num_configs();
 int sellsort_config_unroll(int cfg);

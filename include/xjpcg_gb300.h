@@ -34,7 +34,8 @@ typedef struct {
     uint32_t loopMode;     /* 1 = conditional-graph loop, 0 = host-driven */
     uint32_t spmvLayout;   /* 0 = CSR staged through shared memory, 1 = sliced (SELL-32), 2 = merge path,
                               3 = sliced with int16 column offsets, 4 = sliced with rows sorted by
-                              length (long rows one warp each) */
+                              length (long rows one warp each), 5 = sliced with column offsets
+                              shared by the 32 rows of a slice */
     uint32_t batchThreads; /* batched solves: CTA size chosen by the tuner */
     uint32_t batchLanes;   /* batched solves: lanes per row */
     uint32_t batchSmemRows;/* batched solves: rows of p held in shared memory */
@@ -193,8 +194,9 @@ XJPCG_Status_t xJPCG_gbGetInfo(const XJPCG_Handle_t* handle, XJPCG_GbInfo_t* inf
  * shape[4c..4c+3] = lanes per row, consumer threads per CTA, chunk entries,
  * pipeline stages.  Sliced configurations report (1, 0, unroll, column bits:
  * 32 for absolute int32 columns, 16 for int16 offsets from the row), the
- * length-sorted sliced ones (1, 1, unroll, 32) and the merge-path kernel
- * (0, 256, steps per thread, 0).  At most cap
+ * length-sorted sliced ones (1, 1, unroll, 32), the shared-offset sliced
+ * ones (1, 2, unroll, 0) and the merge-path kernel (0, 256, steps per
+ * thread, 0).  At most cap
  * configurations are written. */
 XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, int32_t* shape, int32_t cap,
                                      int32_t* count);
@@ -212,8 +214,9 @@ XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream);
  * sliced layout, -2 the merge-path kernel, -3 the sliced layout with int16
  * column offsets (INVALID_VALUE when some column lies more than 32767 from
  * its row), -4 the length-sorted sliced layout (INVALID_VALUE when the plain
- * sliced layout pads 20 % or less, where it is not offered); 0 restores
- * tuning.  A forced layout applies to the FP32 SpMV of
+ * sliced layout pads 20 % or less, where it is not offered), -5 the sliced
+ * layout with slice-shared column offsets (INVALID_VALUE when the plain
+ * sliced layout is not available); 0 restores tuning.  A forced layout applies to the FP32 SpMV of
  * the mixed solver as well. */
 XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes);
 

@@ -45,7 +45,7 @@ def test_diffusion27_small_csr(handle):
     _check_solve(s, r)
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32, -1, -2, -3])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32, -1, -2, -3, -5])
 def test_every_spmv_shape_solves(handle, lanes):
     s = W.diffusion27(12, sigma=1.5, seed=7)
     rows, cols, vals = s.coo()
@@ -55,7 +55,7 @@ def test_every_spmv_shape_solves(handle, lanes):
     if lanes > 0:
         assert handle.info().spmvLanes == lanes and handle.info().spmvLayout == 0
     else:
-        assert handle.info().spmvLayout == {-1: 1, -2: 2, -3: 3}[lanes]
+        assert handle.info().spmvLayout == {-1: 1, -2: 2, -3: 3, -5: 5}[lanes]
     _check_solve(s, r)
 
 
@@ -450,4 +450,30 @@ def test_sorted_sliced_not_offered_for_uniform_rows(handle):
     handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
     with pytest.raises(X.XJPCGError):
         handle.set_spmv_lanes(-4)
+    handle.set_spmv_lanes(0)
+
+
+@pytest.mark.parametrize("nx", [9, 40])
+def test_shared_offset_layout_bitwise_equals_sliced(handle, nx):
+    # slices whose rows share the stencil's offsets store them once; boundary
+    # rows get explicit zeros in offset order, so every row sums in its CSR
+    # order exactly as the plain sliced kernel does
+    s = W.diffusion27(nx, seed=11)
+    handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
+    x = np.random.default_rng(nx).standard_normal(s.n)
+    handle.set_spmv_lanes(-1)
+    y1 = handle.spmv(x)
+    handle.set_spmv_lanes(-5)
+    y5 = handle.spmv(x)
+    assert handle.info().spmvLayout == 5
+    assert np.array_equal(y1, y5)
+    r = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    _check_solve(s, r)
+    # values-only update keeps the layout and refreshes its values
+    r = handle.csr_solve(s.n, s.rowptr, s.col, s.val * 2.0, s.diag * 2.0, s.b, 20000, 1e-10,
+                         mode=X.MODE_KEEP_NZ_LAYOUT)
+    assert handle.info().spmvLayout == 5
+    _check_solve(W.System(s.n, s.rowptr, s.col, s.val * 2.0, s.diag * 2.0, s.b), r)
+    m = handle.mixed_solve(s.b, s.diag * 2.0, 20000, 1e-10)
+    assert m.status == X.SUCCESS and handle.info().spmvLayout32 == 5
     handle.set_spmv_lanes(0)
