@@ -36,6 +36,7 @@ WORKLOAD = {"workload": "jpcg_fp64_diffusion27", "grid": "160^3", "n": 4096000, 
             "tol": 1e-10, "max_iter": 20000, "precond": "jacobi", "index": "int32", "dtype": "f64",
             "l2": "inputs larger than L2 (matrix 1.3 GB)"}
 METRIC = "fp64 JPCG time-to-1e-10 relative residual, 27-pt 160^3 (solves/s = 1/time-to-tol)"
+FP64_DFMA_PEAK = 152 * 2 * 2.07e9  # DFMA per second, nominal
 
 
 def parse():
@@ -468,15 +469,18 @@ def run_gb300(args):
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        step_s = []
         for _ in range(args.steps):
+            ts = time.perf_counter()
             e2e_step()
+            step_s.append(time.perf_counter() - ts)
         torch.cuda.synchronize()
         te = max_over_ranks(time.perf_counter() - t0)
         met, inf_e = h.metrics(), h.info()
         e2e = {"value": world * args.steps / te, "unit": "solves/s",
                "h2d_bytes_per_step": int(4 * nnz + 4 * nnz + 8 * nnz + 8 * n + 8 * n),
                "d2h_bytes_per_step": int(8 * n + 256), "time_to_tol_s": te / args.steps,
-               "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays",
+               "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays", "step_s": step_s,
                "last_call_phases_s": {"matProc (H2D, conversion, layouts, tuning)": met.m_matProc,
                                       "of which SpMV tuning": inf_e.tuneMs / 1e3,
                                       "vecProc": met.m_vecProc, "solver (incl. D2H of x)": met.m_solver}}
@@ -520,7 +524,13 @@ def run_gb300(args):
                              "bytes_per_launch": B, "bytes_formula": "(8 + %d) nnz + 4 (n + 1) + 16 n" % col_bytes,
                              "launch_ms": spmv_ms,
                              "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                             "traffic_source": traffic_src},
+                             "traffic_source": traffic_src,
+                             "fp64_issue": {"achieved_gdfma_s": nnz / (spmv_ms / 1e3) / 1e9,
+                                            "peak_gdfma_s": FP64_DFMA_PEAK / 1e9,
+                                            "frac": nnz / (spmv_ms / 1e3) / FP64_DFMA_PEAK,
+                                            "note": "one DFMA per stored entry; peak = nominal 1.25 TFLOP/s fp64 "
+                                                    "(2 DFMA per clock per SM, 152 SMs, 2.07 GHz). The SpMV is "
+                                                    "bound by whichever fraction is higher"}},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clock_info,
                 "loop": "conditional-graph" if h.info().loopMode == 1 else "host"}
         line.update(extras)
