@@ -619,7 +619,7 @@ void PcgHandle::tuneSpmv() {
         best = mergeCfg();
     } else if (m_forcedLanes == -5) {
         if (!ensurePat()) throw InvalidValue("the shared-offset sliced SpMV layout is not offered for this matrix.");
-        best = patCfg0() + 1;  // unroll 8
+        best = patCfg0();  // unroll 4
     } else if (m_forcedLanes == -4) {
         if (!ensureSorted())
             throw InvalidValue("the length-sorted sliced SpMV layout is not offered for this matrix.");
