@@ -558,7 +558,7 @@ bool PcgHandle::ensureSell() {
 }
 
 // Times the SpMV configurations (plain mode, x = p, FP64 or FP32) and returns
-// the fastest.  Sliced layouts go first: on matrices they suit they are the
+// the fastest (-1 when none can launch).  Sliced layouts go first: on matrices they suit they are the
 // fastest, and a good early time lets the rest be judged quickly.  Each
 // configuration gets one launch (warm-up, timed); one that is over 1.5 times
 // the best so far keeps that time, the others get three more and keep the
@@ -566,8 +566,15 @@ bool PcgHandle::ensureSell() {
 int PcgHandle::timeConfigs(bool fp32, std::vector<float>& out) {
     const int ncfg = numSpmvCfgs();
     std::vector<int> order;
-    for (int c = spmv_num_configs(); c < ncfg; ++c) order.push_back(c);
-    for (int c = 0; c < spmv_num_configs(); ++c) order.push_back(c);
+    // Rows of near-uniform length (the sliced copy pads at most 10 %): the
+    // sliced kernels move the fewest bytes with the least overhead, so only
+    // they are timed; the staged-CSR, length-sorted and merge-path kernels
+    // are left out.
+    const bool uniformRows = ensureSell() && m_sellPadRatio <= 1.1;
+    for (int c = spmv_num_configs(); c < ncfg; ++c)
+        if (!uniformRows || isSell(c) || isPat(c)) order.push_back(c);
+    if (!uniformRows)
+        for (int c = 0; c < spmv_num_configs(); ++c) order.push_back(c);
     int best = -1;
     float bestMs = 1e30f;
     for (int c : order) {
