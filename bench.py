@@ -279,7 +279,9 @@ def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
            "oracle": "oracle JPCG to %g (FP64, CPU)" % tight_tol,
            "spmv_layout": LAYOUTS[inf.spmvLayout][0], "spmv_layout_fp32": LAYOUTS[inf.spmvLayout32][0],
            "spmv_fp32_ms": (h.spmv_tuning32()[inf.spmvCfg32] if inf.spmvCfg32 < 64 else None),
-           "spmv_fp64_ms": h.spmv_tuning()[inf.spmvCfg][4]}
+           "spmv_fp64_ms": h.spmv_tuning()[inf.spmvCfg][4],
+           "spmv_fp32_shape": (list(h.spmv_tuning()[inf.spmvCfg32][:4]) if inf.spmvCfg32 < 64 else None),
+           "spmv_tuning_fp32_ms": [round(v, 4) for v in h.spmv_tuning32()]}
     h.close()
     return out
 

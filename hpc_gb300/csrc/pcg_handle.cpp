@@ -343,8 +343,7 @@ bool PcgHandle::ensurePat() {
     alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count(std::max(nslices, n) + 1) + 16), "scan scratch");
     int64_t tot[3] = {0, 0, 0};
     check(sellpat_plan(m_stream, n, m_rowptr.as<int>(), m_col.as<int>(), m_psSliceOff.as<int>(), m_psPatLen.as<int>(),
-                       m_psPatNew.as<int>(), m_psPatIdx.as<int>(), m_psPatOff.as<int>(), m_psGenOff.as<int>(), nullptr,
-                       m_blockSums.as<int>(), tot),
+                       m_psPatNew.as<int>(), m_psPatIdx.as<int>(), m_psGenOff.as<int>(), m_blockSums.as<int>(), tot),
           "shared-offset layout");
     if (tot[0] > 0x7fffff00ll) {
         m_psState = 2;

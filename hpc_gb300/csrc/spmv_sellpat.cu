@@ -61,11 +61,11 @@ __device__ __forceinline__ int warp_sum_int(int v) {
 }
 }  // namespace
 
-// One warp per slice.  info[s] = {stored entries per lane, pattern length
-// (0 = general slice), 1 if the pattern equals the previous slice's}.
+// One warp per slice: stored values of the slice (32 x pattern length for a
+// shared slice, 32 x longest row for a general one), pattern length (0 = a
+// general slice) and general-slice columns.
 __global__ void sp_plan_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
-                               int* __restrict__ lenOut, int* __restrict__ patLen, int* __restrict__ patNew,
-                               int* __restrict__ genLen) {
+                               int* __restrict__ lenOut, int* __restrict__ patLen, int* __restrict__ genLen) {
     const int lane = threadIdx.x & 31;
     const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
     const int nslices = (n + 31) / 32;
@@ -102,7 +102,6 @@ __global__ void sp_plan_kernel(int n, const int* __restrict__ rowptr, const int*
             patLen[s] = shared ? L : 0;
             genLen[s] = shared ? 0 : 32 * maxLen;
         }
-        (void)patNew;
     }
 }
 
@@ -181,8 +180,15 @@ __global__ void sp_fill_kernel(int n, const int* __restrict__ rowptr, const int*
     }
 }
 
+// Unroll 16 keeps twice the loads in flight per warp at 64 registers
+// (4 CTAs per SM); the shallower unrolls fit 40 registers (6 CTAs).
+template <int U>
+struct PatMinBlocks {
+    static constexpr int value = U >= 16 ? 4 : 6;
+};
+
 template <typename VT, int U>
-__global__ void __launch_bounds__(kPatThreads, 6) spmv_sellpat_kernel(
+__global__ void __launch_bounds__(kPatThreads, PatMinBlocks<U>::value) spmv_sellpat_kernel(
     int n, int nslices, const int* __restrict__ sliceOff, const int* __restrict__ patLen,
     const int* __restrict__ patIdx, const int* __restrict__ patOff, const int* __restrict__ genOff,
     const int* __restrict__ pat, const int* __restrict__ gcol, const VT* __restrict__ sval,
@@ -261,20 +267,17 @@ __global__ void __launch_bounds__(kPatThreads, 6) spmv_sellpat_kernel(
 }
 
 // ---- host side ----
-int sellpat_num_configs() { return 2; }
-int sellpat_config_unroll(int cfg) { return cfg == 0 ? 4 : 8; }
+int sellpat_num_configs() { return 3; }
+int sellpat_config_unroll(int cfg) { return cfg == 0 ? 4 : (cfg == 1 ? 8 : 16); }
 
 // Plans the layout.  Per slice (nslices + 1 ints each): sliceOff (values),
-// patLen, patNew, patIdx, patOff (per stored pattern), genOff.  Returns the
-// totals of stored values, pattern entries and general-slice columns, and
-// the number of shared slices.
+// patLen, patNew, patIdx (before sellpat_index: the scan of patNew), genOff.
+// totals = {stored values, general-slice columns, stored patterns}.
 cudaError_t sellpat_plan(cudaStream_t st, int n, const int* rowptr, const int* col, int* sliceOff, int* patLen,
-                         int* patNew, int* patIdx, int* patOff, int* genOff, int* scratch, int* blockSums,
-                         int64_t* totals) {
+                         int* patNew, int* patIdx, int* genOff, int* blockSums, int64_t* totals) {
     const int nslices = (n + 31) / 32;
     const int grid = grid_of((int64_t)nslices * 32, 256);
-    // scratch: nslices + 1 ints
-    sp_plan_kernel<<<grid, 256, 0, st>>>(n, rowptr, col, sliceOff, patLen, patNew, genOff);
+    sp_plan_kernel<<<grid, 256, 0, st>>>(n, rowptr, col, sliceOff, patLen, genOff);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     sp_dedupe_kernel<<<grid, 256, 0, st>>>(n, rowptr, col, patLen, patNew);
@@ -298,7 +301,6 @@ cudaError_t sellpat_plan(cudaStream_t st, int n, const int* rowptr, const int* c
     totals[0] = h[0];
     totals[1] = h[1];
     totals[2] = h[2];  // stored patterns
-    (void)scratch;
     return cudaSuccess;
 }
 
@@ -352,7 +354,8 @@ int sp_bps() {
 
 template <typename VT>
 int sellpat_grid(int cfg, int n, int numSms) {
-    const int bps = sellpat_config_unroll(cfg) == 4 ? sp_bps<VT, 4>() : sp_bps<VT, 8>();
+    const int u = sellpat_config_unroll(cfg);
+    const int bps = u == 4 ? sp_bps<VT, 4>() : (u == 8 ? sp_bps<VT, 8>() : sp_bps<VT, 16>());
     if (bps <= 0) return 0;
     const int nslices = (n + 31) / 32;
     const int need = (nslices + kPatThreads / 32 - 1) / (kPatThreads / 32);
@@ -366,10 +369,15 @@ cudaError_t spmv_sellpat_launch(int cfg, int grid, cudaStream_t st, int n, const
                                 double* partials, int mode, const uint32_t* doneFlag) {
     if (n <= 0) return cudaSuccess;
     const int nslices = (n + 31) / 32;
-    if (sellpat_config_unroll(cfg) == 4)
+    const int u = sellpat_config_unroll(cfg);
+    if (u == 4)
         spmv_sellpat_kernel<VT, 4><<<grid, kPatThreads, 0, st>>>(n, nslices, sliceOff, patLen, patIdx, patOff,
                                                                  genOff, pat, gcol, sval, x, y, b, state, partials,
                                                                  mode, doneFlag);
+    else if (u == 16)
+        spmv_sellpat_kernel<VT, 16><<<grid, kPatThreads, 0, st>>>(n, nslices, sliceOff, patLen, patIdx, patOff,
+                                                                  genOff, pat, gcol, sval, x, y, b, state, partials,
+                                                                  mode, doneFlag);
     else
         spmv_sellpat_kernel<VT, 8><<<grid, kPatThreads, 0, st>>>(n, nslices, sliceOff, patLen, patIdx, patOff,
                                                                  genOff, pat, gcol, sval, x, y, b, state, partials,

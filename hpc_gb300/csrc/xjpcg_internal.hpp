@@ -49,8 +49,7 @@ int sellpat_config_unroll(int cfg);
 // All per-slice arrays hold nslices + 1 ints.  totals = {stored values,
 // general-slice columns, stored patterns}.
 cudaError_t sellpat_plan(cudaStream_t st, int n, const int* rowptr, const int* col, int* sliceOff, int* patLen,
-                         int* patNew, int* patIdx, int* patOff, int* genOff, int* scratch, int* blockSums,
-                         int64_t* totals);
+                         int* patNew, int* patIdx, int* genOff, int* blockSums, int64_t* totals);
 // patOff: nPatterns + 1 ints; *patTotal = stored pattern entries.
 cudaError_t sellpat_index(cudaStream_t st, int n, const int* patLen, const int* patNew, int* patIdx, int nPatterns,
                           int* patOff, int* blockSums, int64_t* patTotal);
