@@ -19,10 +19,10 @@
 //
 // Two precisions share the CG core:
 //   fp64    the xJPCG iteration in FP64 (same arithmetic as cg_kernels.cu).
-//   mixed   FP64 iterative refinement around an FP32 inner CG: r = b - A x in
-//           FP64, inner solve A d = r / ||r|| in FP32 (values, vectors and
-//           per-thread accumulation) to a relative drop innerTol, x += ||r|| d
-//           in FP64; stop when ||b - A x|| <= tol ||b|| (true residual).
+//   mixed   reliable updates: FP32 CG recurrences (values, vectors and
+//           per-thread accumulation) with FP64 refreshes of the true residual
+//           that fold the FP32 increment into the FP64 x; stop when
+//           ||b - A x|| <= tol ||b|| (true residual).
 // Lanes per row (G) and CTA size are template parameters chosen by the host
 // tuner.
 #include <cuda_runtime.h>
@@ -60,9 +60,8 @@ struct BatchArgs {
     uint32_t* queue;
     uint32_t maxIterP1;
     double tol;
-    double innerTol;
+    double delta2;     // mixed: refresh when the FP32 r.r falls below delta2 * its running maximum
     int smemRows;      // p capacity in shared memory (rows)
-    int maxOuter;
 };
 
 template <int NT, int NV, typename T>
@@ -207,10 +206,20 @@ __global__ void __launch_bounds__(NT) batched_fp64_kernel(BatchArgs a) {
     }
 }
 
+// Mixed precision with reliable updates, per system (the batched form of
+// mixed_kernels.cu): the CG recurrences run in FP32 (values, r, p, Ap, J and
+// the increment d; per-thread sums in FP32, CTA sums in FP64) and keep their
+// search direction.  When the FP32 residual norm has fallen by delta below its
+// largest value since the last refresh, looks converged, or the budget is
+// spent, the refresh folds d into the FP64 x, recomputes r = b - A x with the
+// FP64 matrix and restarts the FP32 residual from it.  The system stops on the
+// true FP64 residual: r.r <= b.b tol^2.
 template <int NT, int G>
 __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* pS = reinterpret_cast<float*>(smem);
+    const int tid = threadIdx.x;
+    const int lane = tid % G;
     for (;;) {
         const int sys = next_system(a);
         if (sys < 0) break;
@@ -220,56 +229,117 @@ __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
         const int* rp = a.rowptr + r0;
         const int* cl = a.col + e0;
         const double* vl = a.val + e0;
+        const float* vl32 = a.val32 + e0;
+        float* r = a.r32 + r0;
+        float* d = a.d32 + r0;
+        float* J = a.J32 + r0;
+        float* Ap = a.Ap32 + r0;
+        double* x = a.x + r0;
+        // x = 0, d = 0, J = 1/diag, r = b, p = J r
         double bbA = 0;
-        for (int i = threadIdx.x; i < n; i += NT) {
+        float rzA = 0.f;
+        for (int i = tid; i < n; i += NT) {
             const double bi = a.b[r0 + i];
-            a.x[r0 + i] = 0.0;
-            a.J32[r0 + i] = (float)(1.0 / a.diag[r0 + i]);
+            const float ji = (float)(1.0 / a.diag[r0 + i]);
+            const float ri = (float)bi;
+            x[i] = 0.0;
+            d[i] = 0.f;
+            J[i] = ji;
+            r[i] = ri;
+            P[i] = ji * ri;
             bbA = fma(bi, bi, bbA);
+            rzA = fmaf(ri, ji * ri, rzA);
         }
-        double vb[1] = {bbA};
-        block_allreduce<NT, 1, double>(vb);
-        const double bb = vb[0];
-        uint32_t inner = 0, outer = 0;
-        bool bd = false;
-        double rrTrue = bb;
-        for (;;) {
-            // true residual in FP64: r = b - A x
-            double rrA = 0;
-            for (int row = threadIdx.x; row < n; row += NT) {
-                const int s = rp[row] - e0, e = rp[row + 1] - e0;
-                double acc = 0;
-                for (int q = s; q < e; ++q) acc = fma(vl[q], a.x[r0 + cl[q]], acc);
-                const double ri = a.b[r0 + row] - acc;
-                a.r[r0 + row] = ri;
-                rrA = fma(ri, ri, rrA);
+        double v0[2] = {bbA, (double)rzA};
+        block_allreduce<NT, 2, double>(v0);
+        const double bb = v0[0];
+        const double tols = bb * a.tol * a.tol;
+        double rz = v0[1], rrMax = bb, rrTrue = bb;
+        uint32_t k = 0, outer = 0;
+        bool bd = false, stop = false;
+        while (!stop) {
+            // Ap = A p (FP32), p.Ap
+            float pAp = 0.f;
+            for (int rb = (tid >> 5) * (32 / G); rb < n; rb += NT / G) {
+                const int row = rb + (tid & 31) / G;
+                float acc = 0.f;
+                if (row < n) {
+                    const int s0 = rp[row] - e0, s1 = rp[row + 1] - e0;
+                    for (int q = s0 + lane; q < s1; q += G) acc = fmaf(vl32[q], P[cl[q]], acc);
+                }
+                if (G > 1) {
+#pragma unroll
+                    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+                }
+                if (lane == 0 && row < n) {
+                    Ap[row] = acc;
+                    pAp = fmaf(P[row], acc, pAp);
+                }
             }
-            double vr[1] = {rrA};
-            block_allreduce<NT, 1, double>(vr);
-            rrTrue = vr[0];
-            if (!isfinite(rrTrue)) {
-                bd = true;
-                break;
+            double v1[1] = {(double)pAp};
+            block_allreduce<NT, 1, double>(v1);
+            const double alphaD = rz / v1[0];
+            const float alpha = (float)alphaD;
+            float rrP = 0.f, rzP = 0.f;
+            for (int i = tid; i < n; i += NT) {
+                const float ri = fmaf(-alpha, Ap[i], r[i]);
+                d[i] = fmaf(alpha, P[i], d[i]);
+                r[i] = ri;
+                rrP = fmaf(ri, ri, rrP);
+                rzP = fmaf(ri, ri * J[i], rzP);
             }
-            if (!(rrTrue > bb * a.tol * a.tol) || inner >= a.maxIterP1 - 1u || outer >= (uint32_t)a.maxOuter) break;
-            const double sc = rrTrue > 0 ? 1.0 / sqrt(rrTrue) : 1.0;
-            for (int i = threadIdx.x; i < n; i += NT) a.r32[r0 + i] = (float)(a.r[r0 + i] * sc);
-            __syncthreads();
-            double rrL, rr0;
-            bool bdi;
-            const uint32_t budget = a.maxIterP1 - 1u - inner;
-            const uint32_t k = cg_core<float, NT, G>(n, rp, e0, cl, a.val32 + e0, a.r32 + r0, a.d32 + r0,
-                                                     a.J32 + r0, a.Ap32 + r0, P, a.innerTol, budget, rrL, rr0, bdi);
-            inner += k;
-            ++outer;
-            const double inv = 1.0 / sc;
-            for (int i = threadIdx.x; i < n; i += NT) a.x[r0 + i] = fma((double)a.d32[r0 + i], inv, a.x[r0 + i]);
+            double w[2] = {(double)rrP, (double)rzP};
+            block_allreduce<NT, 2, double>(w);
+            ++k;
+            const double rrN = w[0], rzN = w[1];
+            if (rrN > rrMax) rrMax = rrN;
+            bd = !isfinite(alphaD) || !isfinite(rrN) || !isfinite(rzN);
+            const bool refresh = bd || rrN < a.delta2 * rrMax || rrN < tols || k + 1u >= a.maxIterP1;
+            double beta;
+            if (!refresh) {
+                beta = rzN / rz;
+                rz = rzN;
+            } else {
+                // fold, FP64 true residual, FP32 restart from it
+                for (int i = tid; i < n; i += NT) {
+                    x[i] += (double)d[i];
+                    d[i] = 0.f;
+                }
+                __syncthreads();
+                double rrA = 0;
+                for (int row = tid; row < n; row += NT) {
+                    const int s0 = rp[row] - e0, s1 = rp[row + 1] - e0;
+                    double acc = 0;
+                    for (int q = s0; q < s1; ++q) acc = fma(vl[q], x[cl[q]], acc);
+                    const double ri = a.b[r0 + row] - acc;
+                    r[row] = (float)ri;
+                    rrA = fma(ri, ri, rrA);
+                }
+                __syncthreads();
+                float rzR = 0.f;
+                for (int i = tid; i < n; i += NT) rzR = fmaf(r[i], r[i] * J[i], rzR);
+                double v3[2] = {rrA, (double)rzR};
+                block_allreduce<NT, 2, double>(v3);
+                ++outer;
+                rrTrue = v3[0];
+                rrMax = rrTrue;
+                stop = !(rrTrue > tols) || k + 1u >= a.maxIterP1;
+                if (bd || !isfinite(rrTrue) || !isfinite(v3[1])) {
+                    bd = true;
+                    stop = true;
+                }
+                beta = v3[1] / rz;
+                rz = v3[1];
+            }
+            if (stop) break;
+            const float betaF = (float)beta;
+            for (int i = tid; i < n; i += NT) P[i] = fmaf(betaF, P[i], r[i] * J[i]);
             __syncthreads();
         }
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             BatchResult& o = a.res[sys];
-            o.itersRun = inner;
-            o.iters = inner;
+            o.itersRun = k;
+            o.iters = k;
             o.outer = outer;
             o.res = sqrt(rrTrue / bb);
             o.status = bd ? 1u : 0u;
@@ -388,9 +458,8 @@ cudaError_t batch_launch(int cfg, bool mixed, int numSms, int smemRows, cudaStre
     a.queue = L.queue;
     a.maxIterP1 = L.maxIterP1;
     a.tol = L.tol;
-    a.innerTol = L.innerTol;
+    a.delta2 = L.delta2;
     a.smemRows = smemRows;
-    a.maxOuter = 64;
     const size_t smem = (size_t)smemRows * (mixed ? sizeof(float) : sizeof(double));
     const BatchCfg& c = kBatchCfgs[cfg];
     const int bps = c.bps(mixed, smem);

@@ -1388,7 +1388,10 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
     L.queue = m_bQueue.as<uint32_t>();
     L.maxIterP1 = maxIter + 1u;
     L.tol = tol;
-    L.innerTol = envDouble("XJPCG_INNER_TOL", 1e-5);
+    {
+        const double delta = envDouble("XJPCG_RELIABLE_DELTA", 0.01);
+        L.delta2 = delta * delta;
+    }
 
     // Shape candidates: CTA size x lanes per row x rows of p kept in shared
     // memory (the largest system, or a third of it for more CTAs per SM).

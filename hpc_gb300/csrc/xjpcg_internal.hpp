@@ -155,7 +155,7 @@ struct BatchLaunch {
     uint32_t* queue;
     uint32_t maxIterP1;
     double tol;
-    double innerTol;
+    double delta2;  // mixed: reliable-update threshold, squared
 };
 int batch_num_configs();
 cudaError_t batch_validate_columns(cudaStream_t st, int nsys, const int* sysRow, const int* rowptr, const int* col,
