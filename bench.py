@@ -485,6 +485,7 @@ def run_gb300(args):
                "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays", "step_s": step_s,
                "last_call_phases_s": {"matProc (H2D, conversion, layouts, tuning)": met.m_matProc,
                                       "of which SpMV tuning": inf_e.tuneMs / 1e3,
+                                      "of which H2D of the COO arrays": inf_e.uploadMs / 1e3,
                                       "vecProc": met.m_vecProc, "solver (incl. D2H of x)": met.m_solver}}
 
     cpu = None

@@ -44,6 +44,8 @@ PcgHandle::~PcgHandle() {
     if (m_batchExec) cudaGraphExecDestroy(m_batchExec);
     if (m_ev0) cudaEventDestroy(m_ev0);
     if (m_ev1) cudaEventDestroy(m_ev1);
+    if (m_evUp0) cudaEventDestroy(m_evUp0);
+    if (m_evUp1) cudaEventDestroy(m_evUp1);
     if (m_stream) cudaStreamDestroy(m_stream);
 }
 
@@ -64,6 +66,8 @@ void PcgHandle::init() {
     check(cudaStreamCreateWithFlags(&m_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     check(cudaEventCreate(&m_ev0), "cudaEventCreate");
     check(cudaEventCreate(&m_ev1), "cudaEventCreate");
+    check(cudaEventCreate(&m_evUp0), "cudaEventCreate");
+    check(cudaEventCreate(&m_evUp1), "cudaEventCreate");
     alloc(m_state, sizeof(CgState), "solver state");
     alloc(m_state32, sizeof(CgState), "solver state");
     alloc(m_partials, sizeof(double) * kPartialSlots, "reduction partials");
@@ -85,9 +89,12 @@ void PcgHandle::setCooMat(uint32_t n, uint64_t nnz, const uint32_t* row, const u
     alloc(m_inRow, sizeof(uint32_t) * nnz, "COO rows");
     alloc(m_inCol, sizeof(uint32_t) * nnz, "COO cols");
     alloc(m_inVal, sizeof(double) * nnz, "COO values");
+    check(cudaEventRecord(m_evUp0, m_stream), "event");
     check(cudaMemcpyAsync(m_inRow.p, row, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D rows");
     check(cudaMemcpyAsync(m_inCol.p, col, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D cols");
     check(cudaMemcpyAsync(m_inVal.p, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D values");
+    check(cudaEventRecord(m_evUp1, m_stream), "event");
+    m_uploadTimed = true;
     const uint64_t nnzPad = (nnz + 3) / 4 * 4 + 4;
     alloc(m_rowptr, sizeof(int) * ((size_t)n + 1 + kRowptrPad), "CSR row pointers");
     alloc(m_col, sizeof(int) * nnzPad, "CSR columns");
@@ -1585,6 +1592,8 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->spmvCfg32 = m_spmvCfg32 >= 0 ? (uint32_t)m_spmvCfg32 : 0xffffffffu;
     info->spmvCfg = (uint32_t)m_spmvCfg;
     info->tuneMs = m_lastTuneMs;
+    float up = 0.f;
+    if (m_uploadTimed && cudaEventElapsedTime(&up, m_evUp0, m_evUp1) == cudaSuccess) info->uploadMs = up;
 }
 
 }  // namespace xjpcg

@@ -241,6 +241,8 @@ class PcgHandle {
     uint64_t m_tuned32Gen = ~0ull;
     std::vector<float> m_tuneMs32;
     double m_lastTuneMs = 0.0;  // wall time of the last FP64 tuning
+    cudaEvent_t m_evUp0 = nullptr, m_evUp1 = nullptr;  // around the last COO upload
+    bool m_uploadTimed = false;
 
     // vectors
     uint32_t m_vecN = 0, m_n4 = 0;

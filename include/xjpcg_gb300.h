@@ -46,6 +46,7 @@ typedef struct {
     uint32_t spmvLayout32; /* layout of that configuration, coded as spmvLayout */
     uint32_t reserved;
     double tuneMs;         /* wall time of the last SpMV tuning (part of m_matProc) */
+    double uploadMs;       /* device time of the last COO matrix upload (H2D, part of m_matProc) */
 } XJPCG_GbInfo_t;
 
 /* Per-system outcome of a batched solve. */

@@ -16,6 +16,7 @@ int main(void) {
     F(XJPCG_GbInfo_t, batchMs);
     F(XJPCG_GbInfo_t, spmvCfg32);
     F(XJPCG_GbInfo_t, tuneMs);
+    F(XJPCG_GbInfo_t, uploadMs);
     printf("XJPCG_GbSignature_t=%zu\n", sizeof(XJPCG_GbSignature_t));
     F(XJPCG_GbSignature_t, rowBlocks);
     F(XJPCG_GbSignature_t, rbParamBytes);
