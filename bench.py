@@ -218,9 +218,9 @@ def spmv_bytes(n, nnz, col_bytes=4):
 
 
 def iter_bytes(n, nnz, col_bytes=4):
-    # SpMV + 11 vector streams of 8 B (update: x, p, r, Ap, J read, x, r
-    # written; p kernel: r, J, p read, p written).
-    return spmv_bytes(n, nnz, col_bytes) + 88 * n
+    # SpMV + 10 vector streams of 8 B (update: r, Ap, J read, r written;
+    # p kernel: x, p, r, J read, x, p written).
+    return spmv_bytes(n, nnz, col_bytes) + 80 * n
 
 
 def cpu_sample(sysm, iters_full, sample_iters, nthreads=0):
@@ -471,11 +471,14 @@ def run_gb300(args):
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        step_s = []
+        step_s, step_phases = [], []
         for _ in range(args.steps):
             ts = time.perf_counter()
             e2e_step()
             step_s.append(time.perf_counter() - ts)
+            m_, i_ = h.metrics(), h.info()
+            step_phases.append([round(m_.m_matProc, 4), round(i_.uploadMs / 1e3, 4), round(i_.tuneMs / 1e3, 4),
+                                round(m_.m_solver, 4)])
         torch.cuda.synchronize()
         te = max_over_ranks(time.perf_counter() - t0)
         met, inf_e = h.metrics(), h.info()
@@ -483,6 +486,7 @@ def run_gb300(args):
                "h2d_bytes_per_step": int(4 * nnz + 4 * nnz + 8 * nnz + 8 * n + 8 * n),
                "d2h_bytes_per_step": int(8 * n + 256), "time_to_tol_s": te / args.steps,
                "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays", "step_s": step_s,
+               "step_phases_s": {"columns": ["matProc", "upload", "tuning", "solver"], "steps": step_phases},
                "last_call_phases_s": {"matProc (H2D, conversion, layouts, tuning)": met.m_matProc,
                                       "of which SpMV tuning": inf_e.tuneMs / 1e3,
                                       "of which H2D of the COO arrays": inf_e.uploadMs / 1e3,

@@ -3,15 +3,17 @@
 // Per iteration the loop runs three launches (captured once in a CUDA graph,
 // inside a conditional WHILE node):
 //   1. SpMV + p.Ap + alpha            (spmv_kernels.cu, mode kCgDot)
-//   2. cg_update_kernel: x += alpha p, r -= alpha Ap, z = J r (not stored),
+//   2. cg_update_kernel: r -= alpha Ap, z = J r (not stored),
 //      r.r and r.z reduced over the grid; the last CTA forms beta, writes the
 //      64-byte iteration record, applies the stop rule and sets the loop's
 //      condition.  This fuses the reference's krnl_update_xk (L1/hpc/include/
 //      hw/cgSolver/update_xk.hpp:26-67), krnl_update_rk_jacobi
 //      (update_rk_jacobi.hpp:29-110) and krnl_control (pcg/hw/include/
 //      control.hpp:65-92, tasks.hpp:43-47).
-//   3. cg_pupdate_kernel: p = z + beta p with z = J r recomputed
-//      (update_pk.hpp:26-72).
+//   3. cg_pupdate_kernel: x += alpha p (update_xk.hpp:26-67), then
+//      p = z + beta p with z = J r recomputed (update_pk.hpp:26-72).  x is
+//      updated here rather than in the update kernel so that x and p are
+//      read once per iteration (80 n bytes of vectors instead of 88 n).
 // The vector init kernel restates GenCgVector::init (pcg/sw/include/impl/
 // cgVector.hpp:101-114) and the instruction slot 0 (cgVector.hpp:149-159).
 // Reductions are fixed-order (per-CTA tree, then the last CTA sums the CTA
@@ -86,45 +88,40 @@ __global__ void __launch_bounds__(kVecThreads) cg_init_kernel(int n, int n4, con
     }
 }
 
-__global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, double* __restrict__ x, double* __restrict__ r,
-                                                                const double* __restrict__ p,
-                                                                const double* __restrict__ Ap,
-                                                                const double* __restrict__ J, CgState* state,
-                                                                double* partials) {
+__global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, double* __restrict__ r,
+                                                                   const double* __restrict__ Ap,
+                                                                   const double* __restrict__ J, CgState* state,
+                                                                   double* partials) {
     if (*(volatile uint32_t*)&state->done) {
-        // Only reachable when an earlier kernel of this iteration gave up
-        // (wait timeout); close the loop so the graph cannot spin.
-        if (blockIdx.x == 0 && threadIdx.x == 0 && state->useCond)
-            cudaGraphSetConditional((cudaGraphConditionalHandle)state->condHandle, 0u);
+        // The loop is over (a host-driven batch past convergence, or an
+        // earlier kernel of this iteration gave up on a wait): no x update is
+        // due, and the graph's loop is closed so it cannot spin.
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            state->xSkip = 1u;
+            if (state->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)state->condHandle, 0u);
+        }
         return;
     }
     const double alpha = state->alpha;
     double rr = 0.0, rz = 0.0;
     const int n2 = n4 >> 1;
-    double2* x2 = reinterpret_cast<double2*>(x);
     double2* r2 = reinterpret_cast<double2*>(r);
-    const double2* p2 = reinterpret_cast<const double2*>(p);
     const double2* a2 = reinterpret_cast<const double2*>(Ap);
     const double2* j2 = reinterpret_cast<const double2*>(J);
-    // Two elements per step, all ten loads issued before any arithmetic,
-    // so each thread keeps 160 bytes in flight.
+    // Two elements per step, all six loads issued before any arithmetic.
     const int stride = gridDim.x * blockDim.x;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     for (; i + stride < n2; i += 2 * stride) {
-        double2 xv[2], rv[2], pv[2], av[2], jv[2];
+        double2 rv[2], av[2], jv[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             const int e = i + u * stride;
-            xv[u] = x2[e];
             rv[u] = r2[e];
-            pv[u] = p2[e];
             av[u] = __ldcs(&a2[e]);
             jv[u] = j2[e];
         }
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-            xv[u].x = fma(alpha, pv[u].x, xv[u].x);
-            xv[u].y = fma(alpha, pv[u].y, xv[u].y);
             rv[u].x = fma(-alpha, av[u].x, rv[u].x);
             rv[u].y = fma(-alpha, av[u].y, rv[u].y);
             const double z0 = rv[u].x * jv[u].x, z1 = rv[u].y * jv[u].y;
@@ -132,15 +129,12 @@ __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, doubl
             rr = fma(rv[u].y, rv[u].y, rr);
             rz = fma(rv[u].x, z0, rz);
             rz = fma(rv[u].y, z1, rz);
-            x2[i + u * stride] = xv[u];
             r2[i + u * stride] = rv[u];
         }
     }
     for (; i < n2; i += stride) {
-        double2 xv = x2[i], rv = r2[i];
-        const double2 pv = p2[i], av = __ldcs(&a2[i]), jv = j2[i];
-        xv.x = fma(alpha, pv.x, xv.x);
-        xv.y = fma(alpha, pv.y, xv.y);
+        double2 rv = r2[i];
+        const double2 av = __ldcs(&a2[i]), jv = j2[i];
         rv.x = fma(-alpha, av.x, rv.x);
         rv.y = fma(-alpha, av.y, rv.y);
         const double z0 = rv.x * jv.x, z1 = rv.y * jv.y;
@@ -148,7 +142,6 @@ __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, doubl
         rr = fma(rv.y, rv.y, rr);
         rz = fma(rv.x, z0, rz);
         rz = fma(rv.y, z1, rz);
-        x2[i] = xv;
         r2[i] = rv;
     }
     double v[2] = {rr, rz};
@@ -172,26 +165,37 @@ __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, doubl
         }
         if (s->status & kStatusWaitTimeout) cont = false;
         s->k = k;
+        s->xSkip = 0u;  // this iteration's x += alpha p is due in the p kernel
         s->done = cont ? 0u : 1u;
         if (s->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)s->condHandle, cont ? 1u : 0u);
     }
 }
 
-__global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double* __restrict__ p,
+__global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double* __restrict__ x,
+                                                                 double* __restrict__ p,
                                                                  const double* __restrict__ r,
                                                                  const double* __restrict__ J, CgState* state) {
-    if (*(volatile uint32_t*)&state->done) return;
+    if (*(volatile uint32_t*)&state->xSkip) return;
+    const double alpha = state->alpha;
     const double beta = state->beta;
+    // On the iteration that stopped the loop only x is updated.
+    const bool last = *(volatile uint32_t*)&state->done != 0u;
     const int n2 = n4 >> 1;
+    double2* x2 = reinterpret_cast<double2*>(x);
     double2* p2 = reinterpret_cast<double2*>(p);
     const double2* r2 = reinterpret_cast<const double2*>(r);
     const double2* j2 = reinterpret_cast<const double2*>(J);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
-        double2 pv = p2[i];
-        const double2 rv = r2[i], jv = j2[i];
-        pv.x = fma(beta, pv.x, rv.x * jv.x);
-        pv.y = fma(beta, pv.y, rv.y * jv.y);
-        p2[i] = pv;
+        double2 pv = p2[i], xv = x2[i];
+        xv.x = fma(alpha, pv.x, xv.x);
+        xv.y = fma(alpha, pv.y, xv.y);
+        x2[i] = xv;
+        if (!last) {
+            const double2 rv = r2[i], jv = j2[i];
+            pv.x = fma(beta, pv.x, rv.x * jv.x);
+            pv.y = fma(beta, pv.y, rv.y * jv.y);
+            p2[i] = pv;
+        }
     }
 }
 
@@ -217,15 +221,15 @@ cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const doubl
     return cudaGetLastError();
 }
 
-cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* x, double* r, const double* p,
-                             const double* Ap, const double* J, CgState* state, double* partials) {
-    cg_update_kernel<<<grid, kVecThreads, 0, st>>>(n4, x, r, p, Ap, J, state, partials);
+cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, const double* Ap, const double* J,
+                             CgState* state, double* partials) {
+    cg_update_kernel<<<grid, kVecThreads, 0, st>>>(n4, r, Ap, J, state, partials);
     return cudaGetLastError();
 }
 
-cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* p, const double* r, const double* J,
-                              CgState* state) {
-    cg_pupdate_kernel<<<grid, kVecThreads, 0, st>>>(n4, p, r, J, state);
+cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* r,
+                              const double* J, CgState* state) {
+    cg_pupdate_kernel<<<grid, kVecThreads, 0, st>>>(n4, x, p, r, J, state);
     return cudaGetLastError();
 }
 

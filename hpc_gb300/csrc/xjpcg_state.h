@@ -47,7 +47,7 @@ struct alignas(16) CgState {
     double delta2;                 // mixed precision: refresh when r.r < delta2 * rrMax
     uint64_t relHandle;            // mixed precision: conditional handle of the refresh
     uint32_t skipRefresh;          // mixed precision: 1 = the refresh kernels of this iteration return at once
-    uint32_t pad0;
+    uint32_t xSkip;                // fp64: 1 = the update kernel found the loop done (no x update due)
 };
 
 }  // namespace xjpcg
