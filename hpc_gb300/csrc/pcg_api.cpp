@@ -436,4 +436,10 @@ XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes) {
     XJ_GUARD_END("SpMV lanes set successfully")
 }
 
+XJPCG_Status_t xJPCG_gbSetSpmvConfig(XJPCG_Handle_t* handle, int cfg) {
+    XJ_GUARD_BEGIN
+    p->setSpmvConfig(cfg);
+    XJ_GUARD_END("SpMV configuration set successfully")
+}
+
 }  // extern "C"

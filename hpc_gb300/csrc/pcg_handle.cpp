@@ -77,6 +77,7 @@ void PcgHandle::init() {
     check(cudaStreamSynchronize(m_stream), "sync");
     m_useGraph = envInt("XJPCG_HOST_LOOP", 0) == 0;
     m_forcedLanes = envInt("XJPCG_SPMV_LANES", 0);
+    m_forcedCfg = envInt("XJPCG_SPMV_CFG", -1);
 }
 
 // ---------------------------------------------------------------------------
@@ -277,6 +278,19 @@ void PcgHandle::finishMatrix() {
 void PcgHandle::setLanes(int lanes) {
     m_forcedLanes = lanes;
     if (m_haveMatrix) tuneSpmv();
+}
+
+void PcgHandle::setSpmvConfig(int cfg) {
+    if (cfg < -1) throw InvalidValue("SpMV configuration index must be -1 (tuned) or at least 0.");
+    const int old = m_forcedCfg;
+    m_forcedCfg = cfg;
+    if (!m_haveMatrix) return;
+    try {
+        tuneSpmv();
+    } catch (...) {
+        m_forcedCfg = old;  // a configuration that cannot run is not kept
+        throw;
+    }
 }
 
 // Picks the SpMV configuration by timing every one on the stored matrix
@@ -625,9 +639,10 @@ void PcgHandle::tuneSpmv() {
     const int ncfg = numSpmvCfgs();
     int best = -1;
     float bestMs = 1e30f;
-    const int forcedCfg = envInt("XJPCG_SPMV_CFG", -1);
-    if (forcedCfg >= 0 && forcedCfg < ncfg) {
-        best = forcedCfg;
+    if (m_forcedCfg >= 0) {
+        if (m_forcedCfg >= ncfg || spmvGrid64(m_forcedCfg) <= 0)
+            throw InvalidValue("the forced SpMV configuration is not available for this matrix.");
+        best = m_forcedCfg;
     } else if (m_forcedLanes == -2) {
         best = mergeCfg();
     } else if (m_forcedLanes == -5) {
@@ -707,7 +722,7 @@ void PcgHandle::tuneSpmv32() {
     alloc(m_Ap32, vb32, "Ap32");
     int best = m_spmvCfg;
     m_tuneMs32.assign(ncfg, -1.f);
-    if (m_forcedLanes == 0 && envInt("XJPCG_SPMV_CFG", -1) < 0) {
+    if (m_forcedLanes == 0 && m_forcedCfg < 0) {
         check(cudaMemsetAsync(m_p32.p, 0, vb32, m_stream), "memset");
         const int b32 = timeConfigs(true, m_tuneMs32);
         if (b32 >= 0) best = b32;

@@ -135,6 +135,7 @@ class PcgHandle {
     int tuning(float* ms, int* shape, int cap) const;
     int tuning32(float* ms, int cap) const;
     void setLanes(int lanes);
+    void setSpmvConfig(int cfg);
 
     bool hasMatrix() const { return m_haveMatrix; }
     uint32_t matrixN() const { return m_n; }
@@ -232,6 +233,7 @@ class PcgHandle {
     bool m_sell32Valid = false;
     bool m_val32Valid = false;
     int m_forcedLanes = 0;
+    int m_forcedCfg = -1;  // forced SpMV configuration index, -1 = tuned
     int m_spmvCfg = 2;
     int m_spmvGrid = 0;
     std::vector<float> m_tuneMs;  // median time of each SpMV configuration at the last tuning

@@ -221,6 +221,14 @@ XJPCG_Status_t xJPCG_gbGetStream(const XJPCG_Handle_t* handle, void** stream);
  * the mixed solver as well. */
 XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes);
 
+/* Forces the FP64 SpMV configuration with index cfg of the tuner report
+ * (xJPCG_gbGetSpmvTuning), or restores tuning with -1.  INVALID_VALUE when
+ * the configuration cannot run on the stored matrix (its layout is not
+ * offered); the previous choice then stays.  It takes precedence over
+ * xJPCG_gbSetSpmvLanes.  The FP32 SpMV of the mixed solver uses the same
+ * configuration. */
+XJPCG_Status_t xJPCG_gbSetSpmvConfig(XJPCG_Handle_t* handle, int cfg);
+
 /* y = A x and *d_dot = x.y for callers that cannot allocate device memory.
  *
  * No counterpart in the reference.  Some callers may not allocate at the

@@ -65,6 +65,7 @@ def test_null_handle_paths(built):
     info = X.GbInfo()
     assert lib.xJPCG_gbGetInfo(None, C.byref(info)) == X.NOT_INITIALIZED
     assert lib.xJPCG_gbSetSpmvLanes(None, 4) == X.NOT_INITIALIZED
+    assert lib.xJPCG_gbSetSpmvConfig(None, 0) == X.NOT_INITIALIZED
 
 
 def test_struct_layouts():

@@ -195,6 +195,39 @@ def test_spmv_matches_oracle(handle, lanes):
     assert np.all(np.abs(y - yref) <= 1e-13 * scale)
 
 
+def test_every_forced_config(handle, zipf_small):
+    # every configuration of the tuner report, forced by index: the SpMV
+    # matches the oracle and a solve through it meets the bar; a configuration
+    # whose layout is not offered is refused and the previous choice stays
+    for s in (W.diffusion27(12, seed=9), zipf_small):
+        handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
+        tuning = handle.spmv_tuning()
+        x = np.random.default_rng(3).standard_normal(s.n)
+        yref = oracle.spmv(s.rowptr, s.col, s.val, x)
+        scale = oracle.spmv(s.rowptr, s.col, np.abs(s.val), np.abs(x))
+        ran = 0
+        for c in range(len(tuning)):
+            before = handle.info().spmvCfg
+            try:
+                handle.set_spmv_config(c)
+            except X.XJPCGError as e:
+                assert e.status == X.INVALID_VALUE
+                assert handle.info().spmvCfg == before
+                continue
+            assert handle.info().spmvCfg == c
+            y = handle.spmv(x)
+            assert np.all(np.abs(y - yref) <= 1e-13 * scale), c
+            _check_solve(s, handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10,
+                                             mode=X.MODE_KEEP_MATRIX))
+            ran += 1
+        assert ran >= 11  # the CSR, merge-path and one family of sliced kernels at least
+        with pytest.raises(X.XJPCGError):
+            handle.set_spmv_config(len(tuning))
+        with pytest.raises(X.XJPCGError):
+            handle.set_spmv_config(-2)
+        handle.set_spmv_config(-1)
+
+
 def test_sliced_layout_follows_value_updates(handle):
     s = W.diffusion27(14, seed=6)
     rows, cols, vals = s.coo()
