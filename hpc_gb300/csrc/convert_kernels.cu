@@ -283,6 +283,42 @@ static int grid_for(int64_t work, int threads) {
     return (int)g;
 }
 
+// Order-independent 64-bit fingerprint of a CSR structure: the sum, modulo
+// 2^64, of a mixing function (the splitmix64 finaliser) over (position,
+// column) and (position, row pointer) pairs.  Two structures that differ in any
+// entry get different sums except with probability about 2^-64.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__global__ void struct_hash_kernel(int n, int64_t nnz, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                   unsigned long long* out) {
+    unsigned long long h = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int64_t i = t; i < nnz; i += stride) h += mix64(((unsigned long long)i << 32) ^ (unsigned)col[i]);
+    for (int64_t i = t; i <= n; i += stride)
+        h += mix64((((unsigned long long)i << 32) ^ (unsigned)rowptr[i]) + 0x9e3779b97f4a7c15ull);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+}
+
+cudaError_t struct_hash(cudaStream_t st, int n, int64_t nnz, const int* rowptr, const int* col,
+                        unsigned long long* scratch, uint64_t* hash) {
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    struct_hash_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(n, nnz, rowptr, col, scratch);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    unsigned long long h = 0;
+    if ((e = cudaMemcpyAsync(&h, scratch, sizeof(h), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    *hash = h;
+    return cudaSuccess;
+}
+
 cudaError_t gather_values(cudaStream_t st, int64_t nnz, const uint32_t* perm, const double* src, double* dst) {
     if (nnz <= 0) return cudaSuccess;
     gather_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, perm, src, dst);

@@ -269,7 +269,10 @@ void PcgHandle::finishMatrix() {
     m_ps32Valid = false;
     m_mergeTilesValid = false;
     ++m_structGen;
-    check(cudaStreamSynchronize(m_stream), "sync");
+    alloc(m_hashBuf, 16, "structure fingerprint");
+    check(struct_hash(m_stream, (int)m_n, (int64_t)m_nnz, m_rowptr.as<int>(), m_col.as<int>(),
+                      m_hashBuf.as<unsigned long long>(), &m_structHash),
+          "structure fingerprint");
     m_haveMatrix = true;
     ensureVectors(m_n);
     tuneSpmv();
@@ -638,7 +641,6 @@ void PcgHandle::tuneSpmv() {
     } clk{t0, &m_lastTuneMs};
     const int ncfg = numSpmvCfgs();
     int best = -1;
-    float bestMs = 1e30f;
     if (m_forcedCfg >= 0) {
         if (m_forcedCfg >= ncfg || spmvGrid64(m_forcedCfg) <= 0)
             throw InvalidValue("the forced SpMV configuration is not available for this matrix.");
@@ -663,11 +665,19 @@ void PcgHandle::tuneSpmv() {
         for (int c = spmv_num_configs() - 1; c >= 0; --c)
             if (spmv_config_lanes(c) == m_forcedLanes) best = c;
         if (best < 0) throw InvalidValue("unsupported SpMV lanes per row.");
+    } else if (m_tunedHash == m_structHash && m_tunedCfg >= 0 && m_tunedCfg < ncfg && spmvGrid64(m_tunedCfg) > 0) {
+        // The same structure as the last tuned matrix (row pointers and
+        // columns fingerprinted): SpMV timings depend on the structure only,
+        // so the earlier choice and its table stand.
+        best = m_tunedCfg;
     } else {
         m_tuneMs.assign(ncfg, -1.f);
         check(cudaMemsetAsync(m_p.p, 0, sizeof(double) * m_n4, m_stream), "memset");
         best = timeConfigs(false, m_tuneMs);
         if (best < 0) throw InternalError("no SpMV configuration can be launched on this device.");
+        m_tunedHash = m_structHash;
+        m_tunedCfg = best;
+        m_tuned32Cfg = -1;
     }
     m_spmvCfg = best;
     m_spmvGrid = spmvGrid64(best);
@@ -721,11 +731,16 @@ void PcgHandle::tuneSpmv32() {
     alloc(m_p32, vb32, "p32");
     alloc(m_Ap32, vb32, "Ap32");
     int best = m_spmvCfg;
-    m_tuneMs32.assign(ncfg, -1.f);
     if (m_forcedLanes == 0 && m_forcedCfg < 0) {
-        check(cudaMemsetAsync(m_p32.p, 0, vb32, m_stream), "memset");
-        const int b32 = timeConfigs(true, m_tuneMs32);
-        if (b32 >= 0) best = b32;
+        if (m_tuned32Cfg >= 0 && m_tunedHash == m_structHash && spmvGrid32(m_tuned32Cfg) > 0) {
+            best = m_tuned32Cfg;  // same structure as when it was tuned
+        } else {
+            m_tuneMs32.assign(ncfg, -1.f);
+            check(cudaMemsetAsync(m_p32.p, 0, vb32, m_stream), "memset");
+            const int b32 = timeConfigs(true, m_tuneMs32);
+            if (b32 >= 0) best = b32;
+            if (m_tunedHash == m_structHash) m_tuned32Cfg = best;
+        }
     }
     m_spmvCfg32 = best;
     m_spmvGrid32 = spmvGrid32(best);

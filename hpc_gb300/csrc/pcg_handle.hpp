@@ -234,6 +234,10 @@ class PcgHandle {
     bool m_val32Valid = false;
     int m_forcedLanes = 0;
     int m_forcedCfg = -1;  // forced SpMV configuration index, -1 = tuned
+    // SpMV tuning cache: the choices stand while the structure fingerprint matches
+    DevBuf m_hashBuf;
+    uint64_t m_structHash = 0, m_tunedHash = ~0ull;
+    int m_tunedCfg = -1, m_tuned32Cfg = -1;
     int m_spmvCfg = 2;
     int m_spmvGrid = 0;
     std::vector<float> m_tuneMs;  // median time of each SpMV configuration at the last tuning

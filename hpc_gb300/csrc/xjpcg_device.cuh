@@ -27,25 +27,56 @@ __device__ __forceinline__ T warp_sum(T v) {
 }
 
 // Block-wide sum of NV values per thread; result valid in thread 0.
+//
+// FP64 adds are scarce on this part (about two per clock per SM), so the sum
+// is not a shuffle tree in every warp (five add instructions per value in
+// each of the NT/32 warps).  Every thread stores its value; warp 0 alone adds
+// them, lane l taking l, l + 32, l + 64, ... in that order, and finishes with
+// one shuffle tree: NT/32 + 4 add instructions per value for the whole block.
+// The order is fixed, so results are bitwise stable run to run.
 template <int NT, int NV, typename T>
 __device__ __forceinline__ void block_sum(T (&v)[NV]) {
-    __shared__ T red[NV][NT / 32];
+    __shared__ T part[NV][NT];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
-    if (lane == 0) {
-#pragma unroll
-        for (int i = 0; i < NV; ++i) red[i][wid] = v[i];
-    }
+    for (int i = 0; i < NV; ++i) part[i][threadIdx.x] = v[i];
     __syncthreads();
     if (wid == 0) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            T s = lane < NT / 32 ? red[i][lane] : T(0);
+            T s = part[i][lane];
+#pragma unroll 8
+            for (int w = 1; w < NT / 32; ++w) s += part[i][w * 32 + lane];
             v[i] = warp_sum(s);
         }
     }
     __syncthreads();
+}
+
+// block_sum with the totals returned in every thread.
+template <int NT, int NV, typename T>
+__device__ __forceinline__ void block_allsum(T (&v)[NV]) {
+    __shared__ T part[NV][NT];
+    __shared__ T tot[NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) part[i][threadIdx.x] = v[i];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            T s = part[i][lane];
+#pragma unroll 8
+            for (int w = 1; w < NT / 32; ++w) s += part[i][w * 32 + lane];
+            s = warp_sum(s);
+            if (lane == 0) tot[i] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = tot[i];
+    // the next call's writes to part and tot follow its own first barrier,
+    // which every thread reaches only after this read
 }
 
 // Last-block-done grid reduction of NV doubles.  Each block calls it once with

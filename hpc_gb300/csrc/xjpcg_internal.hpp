@@ -164,6 +164,7 @@ void batch_config_shape(int cfg, int* threads, int* lanes);
 cudaError_t batch_launch(int cfg, bool mixed, int numSms, int smemRows, cudaStream_t st, const BatchLaunch& L,
                          int* gridOut);
 
+
 // ---- partitioned-matrix ("signature") input (signature_kernels.cu) ----
 struct SigChunk {
     int64_t byteStart;   // offset of the chunk in the concatenated channel buffers
@@ -199,6 +200,9 @@ int scan_block_count(int count);
 cudaError_t coo_to_csr(cudaStream_t st, int n, int64_t nnz, const uint32_t* row, const uint32_t* col, int base,
                        int* rowptr, int* colOut, uint32_t* perm, ConvertScratch& scratch, int* hostErr);
 cudaError_t gather_values(cudaStream_t st, int64_t nnz, const uint32_t* perm, const double* src, double* dst);
+// 64-bit fingerprint of a CSR structure (row pointers and columns).
+cudaError_t struct_hash(cudaStream_t st, int n, int64_t nnz, const int* rowptr, const int* col,
+                        unsigned long long* scratch, uint64_t* hash);
 cudaError_t cscsym_expand(cudaStream_t st, int n, int64_t nnzHalf, int64_t nnzFull, const int64_t* rowIdx,
                           const int64_t* colPtr, const double* data, int base, uint32_t* rowOut, uint32_t* colOut,
                           double* valOut, int64_t* posScratch, int* flagScratch, int* blockSums, int* hostErr);

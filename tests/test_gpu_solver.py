@@ -228,6 +228,23 @@ def test_every_forced_config(handle, zipf_small):
         handle.set_spmv_config(-1)
 
 
+def test_tuning_reused_for_same_structure(handle):
+    # a new matrix (MODE_DEFAULT) with the structure of the last tuned one keeps
+    # its SpMV choice without timing again; another structure is timed anew
+    s = W.diffusion27(24, seed=13)
+    r = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
+    _check_solve(s, r)
+    cfg, t1 = handle.info().spmvCfg, handle.info().tuneMs
+    s2 = W.System(s.n, s.rowptr, s.col, s.val * 1.5, s.diag * 1.5, s.b)
+    r = handle.csr_solve(s.n, s2.rowptr, s2.col, s2.val, s2.diag, s2.b, 20000, 1e-10)
+    _check_solve(s2, r)
+    assert handle.info().spmvCfg == cfg and handle.info().tuneMs < t1
+    s3 = W.diffusion27(25, seed=13)
+    r = handle.csr_solve(s3.n, s3.rowptr, s3.col, s3.val, s3.diag, s3.b, 20000, 1e-10)
+    _check_solve(s3, r)
+    assert min(t for t in (e[4] for e in handle.spmv_tuning()) if t > 0) > 0
+
+
 def test_sliced_layout_follows_value_updates(handle):
     s = W.diffusion27(14, seed=6)
     rows, cols, vals = s.coo()
