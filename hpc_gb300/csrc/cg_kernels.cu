@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_init_kernel(int n, int n4, con
     double v[2] = {bb, rz};
     block_sum<kVecThreads, 2, double>(v);
     double fin[2];
-    if (grid_sum_last<2>(v, partials, &state->counters[1], fin) && threadIdx.x == 0) {
+    if (grid_sum_last<kVecThreads, 2>(v, partials, &state->counters[1], fin) && threadIdx.x == 0) {
         CgState* s = state;
         s->bb = fin[0];
         s->rz = fin[1];
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, doubl
     double v[2] = {rr, rz};
     block_sum<kVecThreads, 2, double>(v);
     double fin[2];
-    if (grid_sum_last<2>(v, partials, &state->counters[2], fin) && threadIdx.x == 0) {
+    if (grid_sum_last<kVecThreads, 2>(v, partials, &state->counters[2], fin) && threadIdx.x == 0) {
         CgState* s = state;
         const double rrN = fin[0], rzN = fin[1];
         const double beta = rzN / s->rz;

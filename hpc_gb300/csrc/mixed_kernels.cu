@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kMxThreads) rel_init_kernel(int n, int n4, con
     double v[2] = {bb, (double)rz};
     block_sum<kMxThreads, 2, double>(v);
     double fin[2];
-    if (grid_sum_last<2>(v, partials, &st->counters[1], fin) && threadIdx.x == 0) {
+    if (grid_sum_last<kMxThreads, 2>(v, partials, &st->counters[1], fin) && threadIdx.x == 0) {
         st->bb = fin[0];
         st->rz = fin[1];
         st->rr = fin[0];
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kMxThreads, 5) rel_update_kernel(int n4, float
     float v[2] = {rr, rz};
     block_sum<kMxThreads, 2, float>(v);
     double tot[2] = {(double)v[0], (double)v[1]}, fin[2];
-    if (grid_sum_last<2>(tot, partials, &st->counters[2], fin) && threadIdx.x == 0) {
+    if (grid_sum_last<kMxThreads, 2>(tot, partials, &st->counters[2], fin) && threadIdx.x == 0) {
         const double rrN = fin[0], rzN = fin[1];
         const uint32_t k = st->k + 1u;
         st->k = k;
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kMxThreads) rel_restart_kernel(int n4, const d
     double v[1] = {(double)rz};
     block_sum<kMxThreads, 1, double>(v);
     double fin[1];
-    if (grid_sum_last<1>(v, partials, &st->counters[3], fin) && threadIdx.x == 0) {
+    if (grid_sum_last<kMxThreads, 1>(v, partials, &st->counters[3], fin) && threadIdx.x == 0) {
         const double rrT = st->rrTrue, rzN = fin[0];
         st->outer += 1u;
         st->rr = rrT;

@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(NC + 32) spmv_ws_kernel(int n, int ntiles, con
     AccT v[1] = {dacc};
     block_sum<Sh::NT, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
-    if (grid_sum_last<1>(tot, partials, &state->counters[0], fin)) {
+    if (grid_sum_last<Sh::NT, 1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
             if (mode == kCgDot) {
                 state->pAp = fin[0];
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(kSellThreads, SellMinBlocks<VT, U>::value) spm
     AccT v[1] = {dacc};
     block_sum<kSellThreads, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
-    if (grid_sum_last<1>(tot, partials, &state->counters[0], fin)) {
+    if (grid_sum_last<kSellThreads, 1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
             if (mode == kCgDot) {
                 state->pAp = fin[0];

@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kMT) residual_finish_kernel(int n, const VT* _
     double v[1] = {acc};
     block_sum<kMT, 1, double>(v);
     double fin[1];
-    if (grid_sum_last<1>(v, partials, &state->counters[0], fin) && threadIdx.x == 0) state->rrTrue = fin[0];
+    if (grid_sum_last<kMT, 1>(v, partials, &state->counters[0], fin) && threadIdx.x == 0) state->rrTrue = fin[0];
 }
 
 template <typename VT>

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kThreads) spmv_dot_noalloc_kernel(uint32_t n, 
     double v[1] = {d};
     block_sum<kThreads, 1, double>(v);
     double fin[1];
-    if (grid_sum_last<1>(v, scr->partials, &scr->ticket, fin) && threadIdx.x == 0) *dot = fin[0];
+    if (grid_sum_last<kThreads, 1>(v, scr->partials, &scr->ticket, fin) && threadIdx.x == 0) *dot = fin[0];
 }
 
 std::mutex g_setupMutex;

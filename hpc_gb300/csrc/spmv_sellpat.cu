@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kPatThreads, 6) spmv_sellpat_kernel(
     AccT v[1] = {dacc};
     block_sum<kPatThreads, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
-    if (grid_sum_last<1>(tot, partials, &state->counters[0], fin)) {
+    if (grid_sum_last<kPatThreads, 1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
             if (mode == kSpmvCgDot) {
                 state->pAp = fin[0];

@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kSortThreads) spmv_sellsort_kernel(
     AccT v[1] = {dacc};
     block_sum<kSortThreads, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
-    if (grid_sum_last<1>(tot, partials, &state->counters[0], fin)) {
+    if (grid_sum_last<kSortThreads, 1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
             if (mode == kSpmvCgDot) {
                 state->pAp = fin[0];

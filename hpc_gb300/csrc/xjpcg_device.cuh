@@ -79,11 +79,14 @@ __device__ __forceinline__ void block_allsum(T (&v)[NV]) {
     // which every thread reaches only after this read
 }
 
-// Last-block-done grid reduction of NV doubles.  Each block calls it once with
-// its block total in thread 0.  Returns true in the block that finished last;
-// in that block, out[] holds the grid totals (valid in all threads).  The
-// partial buffer must hold NV * gridDim.x doubles.
-template <int NV>
+// Last-block-done grid reduction of NV doubles.  Each block (NT threads)
+// calls it once with its block total in thread 0.  Returns true in the block
+// that finished last; in that block, out[] holds the grid totals (valid in
+// all threads).  The last block adds the partials with all its threads
+// (thread t takes t, t + NT, ... in order, so every load is in flight at
+// once), then block_sum's fixed order.  The partial buffer must hold
+// NV * gridDim.x doubles.
+template <int NT, int NV>
 __device__ __forceinline__ bool grid_sum_last(const double (&blockTotal)[NV], double* partials,
                                               uint32_t* counter, double (&out)[NV]) {
     __shared__ bool amLast;
@@ -99,16 +102,19 @@ __device__ __forceinline__ bool grid_sum_last(const double (&blockTotal)[NV], do
     __syncthreads();
     if (!amLast) return false;
     __threadfence();
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
+    double s[NV];
 #pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            double s = 0.0;
-            for (int b = lane; b < nb; b += 32) s += __ldcg(&partials[i * nb + b]);
-            s = warp_sum(s);
-            if (lane == 0) fin[i] = s;
-        }
-        if (lane == 0) *counter = 0u;
+    for (int i = 0; i < NV; ++i) {
+        double a = 0.0;
+#pragma unroll 4
+        for (int b = threadIdx.x; b < nb; b += NT) a += __ldcg(&partials[i * nb + b]);
+        s[i] = a;
+    }
+    block_sum<NT, NV, double>(s);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) fin[i] = s[i];
+        *counter = 0u;
     }
     __syncthreads();
 #pragma unroll
