@@ -9,8 +9,10 @@ the path has no data exchange).
   value  inputs resident in HBM: xJPCG_gbSolveDevice on the stored matrix,
          device-timed with CUDA events on the library's stream.
   e2e    the reference-facing call xJPCG_cooSolver(MODE_DEFAULT) from pinned
-         host COO arrays: H2D copies, COO->CSR conversion, SpMV tuning, the
-         solve and the D2H copy of x inside the timed region.
+         host COO arrays: H2D copies, COO->CSR conversion, SpMV layouts and
+         the tuner's choice (timed on the first call, reused while the
+         structure fingerprint matches), the solve and the D2H copy of x
+         inside the timed region; W untimed calls first, as for value.
 
 ``--impl reference`` times the oracle (the C/OpenMP restatement of the
 reference's JPCG; the reference itself only runs on an Alveo U280) on the
