@@ -3,7 +3,7 @@
 // Per iteration the loop runs three launches (captured once in a CUDA graph,
 // inside a conditional WHILE node):
 //   1. SpMV + p.Ap + alpha            (spmv_kernels.cu, mode kCgDot)
-//   2. cg_update_kernel: r -= alpha Ap, z = J r (not stored),
+//   2. cg_update_kernel: r -= alpha Ap, z = J r (written over the spent Ap),
 //      r.r and r.z reduced over the grid; the last CTA forms beta, writes the
 //      64-byte iteration record, applies the stop rule and sets the loop's
 //      condition.  This fuses the reference's krnl_update_xk (L1/hpc/include/
@@ -11,9 +11,10 @@
 //      (update_rk_jacobi.hpp:29-110) and krnl_control (pcg/hw/include/
 //      control.hpp:65-92, tasks.hpp:43-47).
 //   3. cg_pupdate_kernel: x += alpha p (update_xk.hpp:26-67), then
-//      p = z + beta p with z = J r recomputed (update_pk.hpp:26-72).  x is
-//      updated here rather than in the update kernel so that x and p are
-//      read once per iteration (80 n bytes of vectors instead of 88 n).
+//      p = z + beta p with the z the update kernel left (update_pk.hpp:26-72).
+//      x is updated here rather than in the update kernel so that x and p
+//      are read once per iteration; with z stored, an iteration streams 80 n
+//      bytes of vectors (update 40 n, p kernel 40 n) instead of 88 n.
 // The vector init kernel restates GenCgVector::init (pcg/sw/include/impl/
 // cgVector.hpp:101-114) and the instruction slot 0 (cgVector.hpp:149-159).
 // Reductions are fixed-order (per-CTA tree, then the last CTA sums the CTA
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_init_kernel(int n, int n4, con
 }
 
 __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, double* __restrict__ r,
-                                                                   const double* __restrict__ Ap,
+                                                                   double* __restrict__ Ap,
                                                                    const double* __restrict__ J, CgState* state,
                                                                    double* partials) {
     if (*(volatile uint32_t*)&state->done) {
@@ -106,7 +107,7 @@ __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, doubl
     double rr = 0.0, rz = 0.0;
     const int n2 = n4 >> 1;
     double2* r2 = reinterpret_cast<double2*>(r);
-    const double2* a2 = reinterpret_cast<const double2*>(Ap);
+    double2* a2 = reinterpret_cast<double2*>(Ap);
     const double2* j2 = reinterpret_cast<const double2*>(J);
     // Two elements per step, all six loads issued before any arithmetic.
     const int stride = gridDim.x * blockDim.x;
@@ -130,6 +131,7 @@ __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, doubl
             rz = fma(rv[u].x, z0, rz);
             rz = fma(rv[u].y, z1, rz);
             r2[i + u * stride] = rv[u];
+            a2[i + u * stride] = make_double2(z0, z1);  // Ap is spent: z = J r for the p kernel
         }
     }
     for (; i < n2; i += stride) {
@@ -143,6 +145,7 @@ __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, doubl
         rz = fma(rv.x, z0, rz);
         rz = fma(rv.y, z1, rz);
         r2[i] = rv;
+        a2[i] = make_double2(z0, z1);
     }
     double v[2] = {rr, rz};
     block_sum<kVecThreads, 2, double>(v);
@@ -173,8 +176,7 @@ __global__ void __launch_bounds__(kVecThreads, 5) cg_update_kernel(int n4, doubl
 
 __global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double* __restrict__ x,
                                                                  double* __restrict__ p,
-                                                                 const double* __restrict__ r,
-                                                                 const double* __restrict__ J, CgState* state) {
+                                                                 const double* __restrict__ z, CgState* state) {
     if (*(volatile uint32_t*)&state->xSkip) return;
     const double alpha = state->alpha;
     const double beta = state->beta;
@@ -183,17 +185,16 @@ __global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double*
     const int n2 = n4 >> 1;
     double2* x2 = reinterpret_cast<double2*>(x);
     double2* p2 = reinterpret_cast<double2*>(p);
-    const double2* r2 = reinterpret_cast<const double2*>(r);
-    const double2* j2 = reinterpret_cast<const double2*>(J);
+    const double2* z2 = reinterpret_cast<const double2*>(z);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
         double2 pv = p2[i], xv = x2[i];
         xv.x = fma(alpha, pv.x, xv.x);
         xv.y = fma(alpha, pv.y, xv.y);
         x2[i] = xv;
         if (!last) {
-            const double2 rv = r2[i], jv = j2[i];
-            pv.x = fma(beta, pv.x, rv.x * jv.x);
-            pv.y = fma(beta, pv.y, rv.y * jv.y);
+            const double2 zv = z2[i];
+            pv.x = fma(beta, pv.x, zv.x);
+            pv.y = fma(beta, pv.y, zv.y);
             p2[i] = pv;
         }
     }
@@ -221,15 +222,15 @@ cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const doubl
     return cudaGetLastError();
 }
 
-cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, const double* Ap, const double* J,
+cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, double* Ap, const double* J,
                              CgState* state, double* partials) {
     cg_update_kernel<<<grid, kVecThreads, 0, st>>>(n4, r, Ap, J, state, partials);
     return cudaGetLastError();
 }
 
-cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* r,
-                              const double* J, CgState* state) {
-    cg_pupdate_kernel<<<grid, kVecThreads, 0, st>>>(n4, x, p, r, J, state);
+cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* z,
+                              CgState* state) {
+    cg_pupdate_kernel<<<grid, kVecThreads, 0, st>>>(n4, x, p, z, state);
     return cudaGetLastError();
 }
 

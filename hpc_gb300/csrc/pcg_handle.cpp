@@ -826,7 +826,7 @@ void PcgHandle::buildGraph() {
     check(cg_update_launch(update_grid(n4, m_numSms), m_stream, n4, m_r.as<double>(), m_Ap.as<double>(),
                                        m_J.as<double>(), st, part),
           "update kernel");
-    check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
+    check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_Ap.as<double>(), st),
           "p kernel");
     check(cudaStreamEndCapture(m_stream, &body), "capture body end");
     check(cudaGraphInstantiate(&m_exec, g, 0), "graph instantiate");
@@ -876,7 +876,7 @@ Results PcgHandle::run(uint32_t maxIter, double tol) {
                 check(cg_update_launch(update_grid(n4, m_numSms), m_stream, n4, m_r.as<double>(), m_Ap.as<double>(),
                                        m_J.as<double>(), st, part),
                       "update kernel");
-                check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_r.as<double>(), m_J.as<double>(), st),
+                check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_Ap.as<double>(), st),
                       "p kernel");
             }
             ran += 16;

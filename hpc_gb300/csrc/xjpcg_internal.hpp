@@ -107,10 +107,11 @@ int vec_grid(int n4, int numSms);
 int update_grid(int n4, int numSms);
 cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x,
                            double* r, double* p, double* J, double* Ap, CgState* state, double* partials);
-cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, const double* Ap, const double* J,
+// update: r -= alpha Ap, then z = J r is written over Ap; p update reads it
+cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, double* Ap, const double* J,
                              CgState* state, double* partials);
-cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* r,
-                              const double* J, CgState* state);
+cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* z,
+                              CgState* state);
 
 // ---- mixed precision, reliable updates (mixed_kernels.cu) ----
 cudaError_t rel_init_launch(int grid, cudaStream_t s, int n, int n4, const double* b, const double* diag, double* x,
