@@ -37,7 +37,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbCsrSolver", "xJPCG_gbSolveDevice", "xJPCG_gbMixedSolve", "xJPCG_gbSpmv", "xJPCG_gbGetCsr",
     "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes", "xJPCG_gbSetSpmvConfig",
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
-    "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv",
+    "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv", "xJPCG_gbSetSignatureSumOrder",
     "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32",
 ]
 
@@ -127,6 +127,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbEdgeGrad.argtypes = [_P, i64, _P, _P, _P, _P, C.c_int]
     lib.xJPCG_gbSetSignatureMatrix.argtypes = [_P, u32, _P, _P, _P, u64, _P, u64]
     lib.xJPCG_gbSignatureSpmv.argtypes = [_P, _P, u32, _P, u32, u32, _P, u64]
+    lib.xJPCG_gbSetSignatureSumOrder.argtypes = [_P, C.c_int]
     lib.xJPCG_gbExportSignature.argtypes = [_P, _P]
     lib.xJPCG_gbGetSignature.argtypes = [_P, _P, _P, _P]
     lib.xJPCG_gbBatchSolve.argtypes = [_P, u32, _P, _P, _P, _P, _P, _P, _P, u32, dbl, C.c_int, _P, C.c_int]
@@ -349,6 +350,12 @@ class JPCG:
         if st != SUCCESS:
             raise XJPCGError(st, self.last_message())
         self._sig_keep = (bufs, par, rb)
+
+    def set_signature_sum_order(self, order: int):
+        """0: tuned SpMV kernels; 1: the reference FPGA's summation order (bit-exact C semantics)."""
+        st = self.lib.xJPCG_gbSetSignatureSumOrder(self.h, order)
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
 
     def signature_spmv(self, x, y_rows, start_addr=0, frame=False):
         """y = A x on the partitioned matrix; optionally the transY frame."""

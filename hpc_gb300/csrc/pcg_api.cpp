@@ -326,6 +326,12 @@ XJPCG_Status_t xJPCG_gbSignatureSpmv(XJPCG_Handle_t* handle, const double* x, ui
     XJ_GUARD_END("SpMV returns successfully")
 }
 
+XJPCG_Status_t xJPCG_gbSetSignatureSumOrder(XJPCG_Handle_t* handle, int order) {
+    XJ_GUARD_BEGIN
+    p->setSignatureSumOrder(order);
+    XJ_GUARD_END("summation order set successfully")
+}
+
 XJPCG_Status_t xJPCG_gbExportSignature(XJPCG_Handle_t* handle, XJPCG_GbSignature_t* sig) {
     XJ_GUARD_BEGIN
     p->exportSignature(sig);

@@ -269,6 +269,7 @@ void PcgHandle::finishMatrix() {
     m_ps32Valid = false;
     m_mergeTilesValid = false;
     ++m_structGen;
+    ++m_valGen;
     alloc(m_hashBuf, 16, "structure fingerprint");
     check(struct_hash(m_stream, (int)m_n, (int64_t)m_nnz, m_rowptr.as<int>(), m_col.as<int>(),
                       m_hashBuf.as<unsigned long long>(), &m_structHash),
@@ -299,6 +300,7 @@ void PcgHandle::setSpmvConfig(int cfg) {
 // Picks the SpMV configuration by timing every one on the stored matrix
 // (plain mode, x = p buffer), median of three launches each.
 void PcgHandle::refreshSellValues() {
+    ++m_valGen;
     m_sell32Valid = false;
     m_ss32Valid = false;
     if (m_sellState == 1)
@@ -1243,18 +1245,64 @@ void PcgHandle::setSignatureMatrix(uint32_t nch, const void* const* bufs, const 
     m_kind = 4;
     m_sigRows = totalRows;
     finishMatrix();
+    // Run lists for the reference-order SpMV: every run of 32 stored entries
+    // (one row index) listed under its row, in stream order.  The conversion
+    // sorts each row's runs by run index, which is the stream order: the
+    // chunks of a row's channel follow its row block's partitions in order.
+    const int64_t runs = groups / 8;
+    const uint32_t N = (uint32_t)std::max<int64_t>((int64_t)n, runs);
+    alloc(m_sigRunRow, sizeof(uint32_t) * (size_t)runs, "run rows");
+    alloc(m_sigRunIdx, sizeof(uint32_t) * (size_t)runs, "run indices");
+    check(sig_run_rows(m_stream, runs, m_sigRow.as<uint32_t>(), m_sigRunRow.as<uint32_t>(), m_sigRunIdx.as<uint32_t>()),
+          "run rows");
+    alloc(m_sigRunPtr, sizeof(int) * ((size_t)N + 1 + kRowptrPad), "run pointers");
+    alloc(m_sigRunList, sizeof(int) * ((size_t)runs + 8), "run lists");
+    alloc(m_sigRunPerm, sizeof(uint32_t) * ((size_t)runs + 1), "run permutation");
+    alloc(m_counts, sizeof(int) * ((size_t)N + 2), "conversion counts");
+    alloc(m_fill, sizeof(int) * ((size_t)N + 1), "conversion fill");
+    alloc(m_keys, sizeof(uint64_t) * ((size_t)runs + 1), "conversion keys");
+    alloc(m_blockSums, sizeof(int) * ((size_t)scan_block_count((int)std::max<int64_t>((int64_t)N + 1, runs + 1)) + 16),
+          "scan scratch");
+    ConvertScratch rs;
+    rs.counts = m_counts.as<int>();
+    rs.fill = m_fill.as<int>();
+    rs.blockSums = m_blockSums.as<int>();
+    rs.keys = m_keys.as<uint64_t>();
+    rs.flags = m_flags.as<int>();
+    herr = 0;
+    check(coo_to_csr(m_stream, (int)N, runs, m_sigRunRow.as<uint32_t>(), m_sigRunIdx.as<uint32_t>(), 0,
+                     m_sigRunPtr.as<int>(), m_sigRunList.as<int>(), m_sigRunPerm.as<uint32_t>(), rs, &herr),
+          "run lists");
+    if (herr & kStatusIndexError) throw InternalError("run list conversion out of range.");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    m_sigOrderedGen = m_valGen;
+}
+
+void PcgHandle::setSignatureSumOrder(int order) {
+    if (order != 0 && order != 1) throw InvalidValue("summation order must be 0 (fastest) or 1 (the reference's).");
+    m_sigSumOrder = order;
 }
 
 void PcgHandle::signatureSpmv(const double* x, uint32_t xLen, double* y, uint32_t yRows, uint32_t startAddr,
                               unsigned char* frame, uint64_t frameBytes) {
     if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
     if (xLen > m_n || yRows > m_n) throw InvalidValue("vector longer than the matrix.");
+    const bool ordered = m_sigSumOrder == 1;
+    if (ordered && !(m_kind == 4 && m_sigOrderedGen == m_valGen))
+        throw InvalidValue("the reference-order SpMV needs a matrix loaded by xJPCG_gbSetSignatureMatrix and "
+                           "unchanged since.");
     alloc(m_scratchY, sizeof(double) * ((size_t)m_n4 + 4), "SpMV output");
     check(cudaMemsetAsync(m_b.p, 0, sizeof(double) * m_n4, m_stream), "memset");
     check(cudaMemcpyAsync(m_b.p, x, sizeof(double) * xLen, cudaMemcpyHostToDevice, m_stream), "H2D x");
-    check(spmv64(m_spmvCfg, m_spmvGrid, m_b.as<double>(), m_scratchY.as<double>(), nullptr, m_state.as<CgState>(),
-                 m_partials.as<double>(), kSpmvPlain, nullptr),
-          "SpMV");
+    if (ordered)
+        check(sig_ordered_spmv(m_stream, (int)m_n, m_sigRunPtr.as<int>(), m_sigRunList.as<int>(),
+                               m_sigVal.as<double>(), m_sigCol.as<uint32_t>(), m_b.as<double>(),
+                               m_scratchY.as<double>()),
+              "reference-order SpMV");
+    else
+        check(spmv64(m_spmvCfg, m_spmvGrid, m_b.as<double>(), m_scratchY.as<double>(), nullptr,
+                     m_state.as<CgState>(), m_partials.as<double>(), kSpmvPlain, nullptr),
+              "SpMV");
     if (y) check(cudaMemcpyAsync(y, m_scratchY.p, sizeof(double) * yRows, cudaMemcpyDeviceToHost, m_stream), "D2H y");
     if (frame) {
         const uint64_t need = 64 + 64 * (uint64_t)(yRows == 0 ? 1 : (yRows + 7) / 8);

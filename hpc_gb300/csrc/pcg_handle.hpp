@@ -114,6 +114,7 @@ class PcgHandle {
     // The reference's partitioned-matrix buffers as the stored matrix.
     void setSignatureMatrix(uint32_t nch, const void* const* bufs, const uint64_t* bytes, const void* par,
                             uint64_t parBytes, const void* rb, uint64_t rbBytes);
+    void setSignatureSumOrder(int order);
     void signatureSpmv(const double* x, uint32_t xLen, double* y, uint32_t yRows, uint32_t startAddr,
                        unsigned char* frame, uint64_t frameBytes);
     uint32_t sigRows() const { return m_sigRows; }
@@ -262,6 +263,10 @@ class PcgHandle {
     // signature input
     DevBuf m_sigBuf, m_sigChunks, m_sigRow, m_sigCol, m_sigVal, m_sigKeep, m_sigFrame;
     uint32_t m_sigRows = 0;
+    // reference-order SpMV over the decoded stored entries (m_sigVal, m_sigCol)
+    DevBuf m_sigRunRow, m_sigRunIdx, m_sigRunPtr, m_sigRunList, m_sigRunPerm;
+    int m_sigSumOrder = 0;                         // 0 = fastest SpMV, 1 = the reference's summation order
+    uint64_t m_valGen = 0, m_sigOrderedGen = ~0ull;  // matrix values generation; the one the run lists match
     SigExport m_sigExport;
     uint64_t m_structGen = 0;  // bumped whenever a new matrix structure is stored
     // adjoint

@@ -77,6 +77,70 @@ __global__ void sig_compact_kernel(int64_t count, const int* __restrict__ pos, c
     }
 }
 
+// ---------------------------------------------------------------------------
+// SpMV in the reference FPGA's summation order.
+//
+// The reference's SpMV (L1/sparse/include/hw/xf_sparse/fp64) adds in a fixed
+// order that its C source spells out:
+//   multAddX  (spmv.hpp:136-157)  each group of 4 stored entries: the four
+//             products v_j * x_j, each rounded, summed left to right from 0;
+//   regAcc    (spmv.hpp:159-185)  each run of 8 such group sums (the 32
+//             entries under one row index) summed left to right from 0;
+//   rowMemAcc (spmv.hpp:452-476)  each row's run sums added to its row store,
+//             which starts at 0, in the order the channel stream holds them
+//             (its row block's partitions in order);
+//   accY      (dataMovers.hpp:339-375)  the 16 channels' row values summed
+//             from 0 in channel order; a row lives in one channel, the other
+//             fifteen give +0, so y = 0 + (the row store).
+// Multiplies and adds are issued separately with round-to-nearest (no fused
+// multiply-add), so the GPU result is the C semantics of that source bit for
+// bit.  One thread per row walks its runs (32 stored entries each) in stream
+// order; the run lists are built once when the matrix is loaded.
+__global__ void sig_run_rows_kernel(int64_t runs, const uint32_t* __restrict__ row, uint32_t* __restrict__ runRow,
+                                    uint32_t* __restrict__ runIdx) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < runs; k += (int64_t)gridDim.x * blockDim.x) {
+        runRow[k] = row[32 * k];
+        runIdx[k] = (uint32_t)k;
+    }
+}
+
+__global__ void sig_ordered_spmv_kernel(int rows, const int* __restrict__ runPtr, const int* __restrict__ runIdx,
+                                        const double* __restrict__ val, const uint32_t* __restrict__ col,
+                                        const double* __restrict__ x, double* __restrict__ y) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+        double store = 0.0;
+        for (int k = runPtr[i]; k < runPtr[i + 1]; ++k) {
+            const int64_t e0 = 32 * (int64_t)runIdx[k];
+            double run = 0.0;
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                double grp = 0.0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int64_t e = e0 + 4 * b + j;
+                    grp = __dadd_rn(grp, __dmul_rn(val[e], x[col[e]]));
+                }
+                run = __dadd_rn(run, grp);
+            }
+            store = __dadd_rn(store, run);
+        }
+        y[i] = __dadd_rn(0.0, store);
+    }
+}
+
+cudaError_t sig_run_rows(cudaStream_t st, int64_t runs, const uint32_t* row, uint32_t* runRow, uint32_t* runIdx) {
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((runs + 255) / 256, 152 * 16));
+    sig_run_rows_kernel<<<grid, 256, 0, st>>>(runs, row, runRow, runIdx);
+    return cudaGetLastError();
+}
+
+cudaError_t sig_ordered_spmv(cudaStream_t st, int rows, const int* runPtr, const int* runIdx, const double* val,
+                             const uint32_t* col, const double* x, double* y) {
+    const int grid = std::max(1, std::min((rows + 127) / 128, 152 * 16));
+    sig_ordered_spmv_kernel<<<grid, 128, 0, st>>>(rows, runPtr, runIdx, val, col, x, y);
+    return cudaGetLastError();
+}
+
 cudaError_t sig_decode(cudaStream_t st, int nchunks, const SigChunk* chunks, const unsigned char* buf, int64_t groups,
                        uint32_t* row, uint32_t* col, double* val, int* keep) {
     if (groups <= 0) return cudaSuccess;

@@ -178,6 +178,11 @@ cudaError_t sig_decode(cudaStream_t st, int nchunks, const SigChunk* chunks, con
 cudaError_t sig_compact(cudaStream_t st, int64_t count, const int* pos, const int* keep, const uint32_t* row,
                         const uint32_t* col, const double* val, uint32_t* rowOut, uint32_t* colOut, double* valOut);
 cudaError_t transy_frame(cudaStream_t st, uint32_t startAddr, uint32_t rows, const double* y, unsigned char* frame);
+// runs of 32 stored entries (one row index each): their rows and indices
+cudaError_t sig_run_rows(cudaStream_t st, int64_t runs, const uint32_t* row, uint32_t* runRow, uint32_t* runIdx);
+// y = A x in the reference FPGA's summation order over the decoded stored entries
+cudaError_t sig_ordered_spmv(cudaStream_t st, int rows, const int* runPtr, const int* runIdx, const double* val,
+                             const uint32_t* col, const double* x, double* y);
 
 // ---- adjoint (adjoint_kernels.cu) ----
 cudaError_t grad_nnz_launch(cudaStream_t st, int n, const int* rowptr, const int* col, const uint32_t* perm,

@@ -136,6 +136,18 @@ XJPCG_Status_t xJPCG_gbGetSignature(XJPCG_Handle_t* handle, void* rbParam, void*
 XJPCG_Status_t xJPCG_gbSignatureSpmv(XJPCG_Handle_t* handle, const double* x, uint32_t xLen, double* y,
                                      uint32_t yRows, uint32_t startAddr, void* frame, uint64_t frameBytes);
 
+/* Summation order of xJPCG_gbSignatureSpmv.  0 (the default): the tuned SpMV
+ * kernels, each row summed in its CSR order with fused multiply-adds.
+ * 1: the order of the reference's FPGA SpMV as its C source states it
+ * (L1/sparse/include/hw/xf_sparse/fp64/spmv.hpp multAddX 136-157, regAcc
+ * 159-185, rowMemAcc 452-476; dataMovers.hpp accY 339-375): each group of 4
+ * stored entries as four rounded products summed left to right, each run of
+ * 8 groups summed left to right, each row's runs in stream order, plus 0;
+ * padding entries included.  Order 1 needs a matrix loaded by
+ * xJPCG_gbSetSignatureMatrix and unchanged since (INVALID_VALUE otherwise),
+ * and gives the same bits as a C execution of that source. */
+XJPCG_Status_t xJPCG_gbSetSignatureSumOrder(XJPCG_Handle_t* handle, int order);
+
 /* Adjoint of the handle's last solve x = A^-1 b (no counterpart in the
  * reference).  With g = dL/dx, solves lambda = A^-1 g (A is SPD) with the
  * same fp64 JPCG and stop rule, then, when gradA is not NULL, writes

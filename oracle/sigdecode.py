@@ -55,6 +55,17 @@ def decode(path: str):
     row, col, val, channel, part (global partition id), pos (index within its
     channel chunk), plus 'info' (m, n, nnz, mPad, nPad, nnzPad)."""
     rb, par, nnz, info = read_signature(path)
+    res = decode_bytes(rb, par, nnz)
+    res["info"] = info
+    return res
+
+
+def decode_bytes(rb: bytes, par: bytes, nnz):
+    """decode() over the rbParam, parParam and 16 nnzVal buffers in memory.
+    Entries come in stream order: row block, then channel, then partition,
+    then position in the channel chunk."""
+    rb, par = bytes(rb), bytes(par)
+    nnz = [bytes(b) for b in nnz]
     total_rows, total_rbs = _u32(rb, 0, 2)
     total_pars = int(_u32(par, 0, 1)[0])
     idx_width = MEM_BYTES // 2
@@ -102,9 +113,72 @@ def decode(path: str):
         s_par += int(npars)
     assert s_par == total_pars
     res = {k: np.array(v) for k, v in out.items()}
-    res["info"] = info
     res["total_rows"] = int(total_rows)
     return res
+
+
+def fpga_order_spmv(dec, x, rows: int):
+    """y = A x (first `rows` rows) in the summation order the reference's FPGA
+    SpMV spells out in its C source, over every stored entry of a decoded
+    signature (padding included, stream order):
+
+    - multAddX (L1/sparse/include/hw/xf_sparse/fp64/spmv.hpp:136-157): each
+      group of 4 stored entries, the products v_j * x_j (each rounded) summed
+      left to right from 0;
+    - regAcc (spmv.hpp:159-185): each run of 8 group sums (the 32 entries under
+      one row index) summed left to right from 0;
+    - rowMemAcc (spmv.hpp:452-476): a row's run sums added to its row store,
+      which starts at 0, in stream order (its row block's partitions in order);
+    - accY (dataMovers.hpp:339-375): the 16 channels' values for the row summed
+      from 0 in channel order; a row belongs to one channel and the others give
+      +0, so y = 0 + (row store).
+
+    Every operation is a separate IEEE double multiply or add (numpy
+    elementwise), so the result is the C semantics of that source."""
+    val = np.asarray(dec["val"], np.float64)
+    col = np.asarray(dec["col"], np.int64)
+    row = np.asarray(dec["row"], np.int64)
+    xp = np.zeros(max(int(col.max()) + 1, len(x)), np.float64)
+    xp[:len(x)] = x
+    prod = val * xp[col]
+    p4 = prod.reshape(-1, 4)
+    grp = 0.0 + p4[:, 0]
+    for j in range(1, 4):
+        grp = grp + p4[:, j]
+    g8 = grp.reshape(-1, 8)
+    run = 0.0 + g8[:, 0]
+    for j in range(1, 8):
+        run = run + g8[:, j]
+    run_row = row[::32]
+    order = np.argsort(run_row, kind="stable")  # keeps stream order within a row
+    rr, rv = run_row[order], run[order]
+    first = np.searchsorted(rr, rr, side="left")
+    k = np.arange(rr.size) - first  # position of the run within its row
+    nrow = max(rows, int(run_row.max()) + 1)
+    store = np.zeros(nrow, np.float64)
+    for step in range(int(k.max()) + 1 if k.size else 0):
+        m = k == step
+        store[rr[m]] = store[rr[m]] + rv[m]
+    return (0.0 + store)[:rows]
+
+
+def fpga_order_spmv_literal(dec, x, rows: int):
+    """fpga_order_spmv written as the plain loops of the reference source
+    (small cases only; pins the vectorised form)."""
+    val, col, row = dec["val"], dec["col"], dec["row"]
+    store = {}
+    for r0 in range(0, len(val), 32):
+        run = 0.0
+        for b in range(8):
+            grp = 0.0
+            for j in range(4):
+                e = r0 + 4 * b + j
+                xv = float(x[col[e]]) if col[e] < len(x) else 0.0
+                grp += float(val[e]) * xv
+            run += grp
+        r = int(row[r0])
+        store[r] = store.get(r, 0.0) + run
+    return np.array([0.0 + store.get(i, 0.0) for i in range(rows)])
 
 
 def stored_order(dec):
