@@ -35,7 +35,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_getErrorString", "xJPCG_createHandle", "xJPCG_destroyHandle", "xJPCG_cscSymSolver",
     "xJPCG_cooSolver", "xJPCG_peekAtLastStatus", "xJPCG_getLastMessage", "xJPCG_getMetrics",
     "xJPCG_gbCsrSolver", "xJPCG_gbSolveDevice", "xJPCG_gbMixedSolve", "xJPCG_gbSpmv", "xJPCG_gbGetCsr",
-    "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes", "xJPCG_gbSetSpmvConfig",
+    "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes", "xJPCG_gbSetSpmvConfig", "xJPCG_gbSetSpmvConfig32",
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
     "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv", "xJPCG_gbSetSignatureSumOrder",
     "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32",
@@ -120,6 +120,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbGetStream.argtypes = [_P, C.POINTER(_P)]
     lib.xJPCG_gbSetSpmvLanes.argtypes = [_P, C.c_int]
     lib.xJPCG_gbSetSpmvConfig.argtypes = [_P, C.c_int]
+    lib.xJPCG_gbSetSpmvConfig32.argtypes = [_P, C.c_int]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbGetSpmvTuning32.argtypes = [_P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
@@ -418,6 +419,12 @@ class JPCG:
 
     def set_spmv_lanes(self, lanes: int):
         st = self.lib.xJPCG_gbSetSpmvLanes(self.h, lanes)
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+
+    def set_spmv_config32(self, cfg: int):
+        """Force the mixed solver's FP32 SpMV configuration (index of spmv_tuning(); -1: tuned)."""
+        st = self.lib.xJPCG_gbSetSpmvConfig32(self.h, cfg)
         if st != SUCCESS:
             raise XJPCGError(st, self.last_message())
 

@@ -448,4 +448,10 @@ XJPCG_Status_t xJPCG_gbSetSpmvConfig(XJPCG_Handle_t* handle, int cfg) {
     XJ_GUARD_END("SpMV configuration set successfully")
 }
 
+XJPCG_Status_t xJPCG_gbSetSpmvConfig32(XJPCG_Handle_t* handle, int cfg) {
+    XJ_GUARD_BEGIN
+    p->setSpmvConfig32(cfg);
+    XJ_GUARD_END("FP32 SpMV configuration set successfully")
+}
+
 }  // extern "C"

@@ -284,6 +284,13 @@ void PcgHandle::setLanes(int lanes) {
     if (m_haveMatrix) tuneSpmv();
 }
 
+void PcgHandle::setSpmvConfig32(int cfg) {
+    if (cfg < -1) throw InvalidValue("SpMV configuration index must be -1 (tuned) or at least 0.");
+    if (cfg >= numSpmvCfgs()) throw InvalidValue("no such SpMV configuration.");
+    m_forcedCfg32 = cfg;
+    m_tuned32Gen = ~0ull;  // chosen again at the next mixed solve
+}
+
 void PcgHandle::setSpmvConfig(int cfg) {
     if (cfg < -1) throw InvalidValue("SpMV configuration index must be -1 (tuned) or at least 0.");
     const int old = m_forcedCfg;
@@ -733,7 +740,11 @@ void PcgHandle::tuneSpmv32() {
     alloc(m_p32, vb32, "p32");
     alloc(m_Ap32, vb32, "Ap32");
     int best = m_spmvCfg;
-    if (m_forcedLanes == 0 && m_forcedCfg < 0) {
+    if (m_forcedCfg32 >= 0) {
+        if (m_forcedCfg32 >= ncfg || spmvGrid32(m_forcedCfg32) <= 0)
+            throw InvalidValue("the forced FP32 SpMV configuration is not available for this matrix.");
+        best = m_forcedCfg32;
+    } else if (m_forcedLanes == 0 && m_forcedCfg < 0) {
         if (m_tuned32Cfg >= 0 && m_tunedHash == m_structHash && spmvGrid32(m_tuned32Cfg) > 0) {
             best = m_tuned32Cfg;  // same structure as when it was tuned
         } else {

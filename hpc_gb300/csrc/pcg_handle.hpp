@@ -137,6 +137,7 @@ class PcgHandle {
     int tuning32(float* ms, int cap) const;
     void setLanes(int lanes);
     void setSpmvConfig(int cfg);
+    void setSpmvConfig32(int cfg);
 
     bool hasMatrix() const { return m_haveMatrix; }
     uint32_t matrixN() const { return m_n; }
@@ -235,6 +236,7 @@ class PcgHandle {
     bool m_val32Valid = false;
     int m_forcedLanes = 0;
     int m_forcedCfg = -1;  // forced SpMV configuration index, -1 = tuned
+    int m_forcedCfg32 = -1;  // forced FP32 SpMV configuration of the mixed solver, -1 = tuned
     // SpMV tuning cache: the choices stand while the structure fingerprint matches
     DevBuf m_hashBuf;
     uint64_t m_structHash = 0, m_tunedHash = ~0ull;

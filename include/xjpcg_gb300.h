@@ -241,6 +241,12 @@ XJPCG_Status_t xJPCG_gbSetSpmvLanes(XJPCG_Handle_t* handle, int lanes);
  * configuration. */
 XJPCG_Status_t xJPCG_gbSetSpmvConfig(XJPCG_Handle_t* handle, int cfg);
 
+/* Forces the mixed solver's FP32 SpMV configuration (index cfg of the tuner
+ * report; -1 restores tuning).  It applies from the next mixed solve, which
+ * fails with INVALID_VALUE when the configuration cannot run on the stored
+ * matrix in FP32. */
+XJPCG_Status_t xJPCG_gbSetSpmvConfig32(XJPCG_Handle_t* handle, int cfg);
+
 /* y = A x and *d_dot = x.y for callers that cannot allocate device memory.
  *
  * No counterpart in the reference.  Some callers may not allocate at the

@@ -66,6 +66,8 @@ def test_null_handle_paths(built):
     assert lib.xJPCG_gbGetInfo(None, C.byref(info)) == X.NOT_INITIALIZED
     assert lib.xJPCG_gbSetSpmvLanes(None, 4) == X.NOT_INITIALIZED
     assert lib.xJPCG_gbSetSpmvConfig(None, 0) == X.NOT_INITIALIZED
+    assert lib.xJPCG_gbSetSpmvConfig32(None, 0) == X.NOT_INITIALIZED
+    assert lib.xJPCG_gbSetSignatureSumOrder(None, 1) == X.NOT_INITIALIZED
 
 
 def test_struct_layouts():

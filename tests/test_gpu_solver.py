@@ -228,6 +228,27 @@ def test_every_forced_config(handle, zipf_small):
         handle.set_spmv_config(-1)
 
 
+def test_forced_fp32_config_same_bits(handle):
+    # the mixed solver's FP32 SpMV forced to each shared-offset form: the
+    # unroll does not change the order of a row's FMAs, so the mixed solves
+    # agree bit for bit; a configuration index out of range is refused
+    s = W.diffusion27(30, seed=14)
+    handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
+    shapes = [t[:4] for t in handle.spmv_tuning()]
+    cfgs = [shapes.index((1, 2, u, 0)) for u in (4, 8)]
+    out = []
+    for c in cfgs:
+        handle.set_spmv_config32(c)
+        m = handle.mixed_solve(s.b, s.diag, 20000, 1e-10)
+        assert m.status == X.SUCCESS and handle.info().spmvCfg32 == c
+        out.append((m.iters, m.x.copy()))
+    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
+    assert oracle.true_relres(s.rowptr, s.col, s.val, s.b, out[0][1]) <= RES_TOL * 1.5
+    with pytest.raises(X.XJPCGError):
+        handle.set_spmv_config32(len(shapes))
+    handle.set_spmv_config32(-1)
+
+
 def test_tuning_reused_for_same_structure(handle):
     # a new matrix (MODE_DEFAULT) with the structure of the last tuned one keeps
     # its SpMV choice without timing again; another structure is timed anew
