@@ -134,3 +134,16 @@ def true_relres(rowptr, col, val, b, x, nthreads=0) -> float:
     n = rowptr.size - 1
     return lib().orc_true_relres(n, _p(rowptr), _p(col), _p(val), _p(np.ascontiguousarray(b, np.float64)),
                                  _p(np.ascontiguousarray(x, np.float64)), nthreads)
+
+
+def ref_mismatches(x, ref, rtol=1e-4, atol=3e-6) -> int:
+    """Mismatch count of the reference's test compare for doubles
+    (utils/include/sw/utils.hpp:82-97, compare<double> -> isClose<float>(1e-4,
+    3e-6)): both values are taken to float and |x - ref| <= atol + rtol |ref| is
+    evaluated in float.  pcgtest.cpp:115-116 and the SpMV test
+    (L2/sparse/tests/fp64/spmv/main.cpp:180-190) pass on zero mismatches."""
+    xf = np.asarray(x, np.float64).astype(np.float32)
+    rf = np.asarray(ref, np.float64).astype(np.float32)
+    diff = np.abs(xf - rf)
+    bound = np.float32(atol) + np.float32(rtol) * np.abs(rf)
+    return int(np.count_nonzero(~(diff <= bound)))

@@ -95,3 +95,11 @@ def test_values_only_update_slots(path):
         _, _, v2 = oracle.cscsym_expand(int(g["n"]), g["rowidx"], g["colptr"], g["data2"], base=int(g["base"]))
         new = v2[pm]
     assert np.array_equal(new, g["sig2_val"])
+
+
+def test_reference_compare_rule():
+    # utils/include/sw/utils.hpp:82-97: float |x - ref| <= 3e-6 + 1e-4 |ref|
+    x = np.array([1.0, 1.00011, 0.0, 1e-7, 1e5 + 9.0, 1e5 + 11.0])
+    ref = np.array([1.0, 1.0, 2e-6, 0.0, 1e5, 1e5])
+    assert oracle.ref_mismatches(x, ref) == 2  # 1.00011 vs 1, and 1e5 + 11 vs 1e5
+    assert oracle.ref_mismatches(x[:1], ref[:1]) == 0

@@ -249,6 +249,42 @@ def test_forced_fp32_config_same_bits(handle):
     handle.set_spmv_config32(-1)
 
 
+@pytest.mark.parametrize("case", ["poisson7_24", "diffusion27_20", "zipf_30k"])
+def test_pcgtest_flow_known_x(handle, case, zipf_small):
+    # pcg/sw/tests/pcgtest.cpp:104-135 with pcg/sw/utils/genMat.py:38-98 data:
+    # x = rand(n), b = A x, diag from the matrix; maxIter 5000, tol 1e-12
+    # (runAllPcgTests.sh); a DEFAULT solve, then KEEP_NZ_LAYOUT re-solves;
+    # each passes on zero mismatches of the reference's compare against x, or
+    # when the solve ran to maxIter
+    s = {"poisson7_24": lambda: W.poisson7(24), "diffusion27_20": lambda: W.diffusion27(20, seed=15),
+         "zipf_30k": lambda: zipf_small}[case]()
+    rng = np.random.default_rng(16)
+    x_true = rng.random(s.n)
+    b = oracle.spmv(s.rowptr, s.col, s.val, x_true)
+    rows, cols, vals = s.coo()
+    for run in range(3):
+        mode = X.MODE_DEFAULT if run == 0 else X.MODE_KEEP_NZ_LAYOUT
+        r = handle.coo_solve(s.n, rows if run == 0 else None, cols if run == 0 else None, vals, s.diag, b,
+                             5000, 1e-12, mode=mode, nnz=len(vals))
+        assert r.status in (X.SUCCESS, X.EXECUTION_FAILED), r.message
+        assert oracle.ref_mismatches(r.x, x_true) == 0 or r.iters == 5000, (run, r.iters)
+
+
+def test_spmv_gen_vectors_refvec(handle):
+    # L2/sparse/tests/fp64/spmv/python/gen_vectors.py:43-67: refVec =
+    # scipy coo.dot(x) with x = rand; the SpMV run passes on zero mismatches of
+    # the reference's compare (main.cpp:180-190)
+    sp = pytest.importorskip("scipy.sparse")
+    s = W.diffusion27(18, seed=17)
+    rows, cols, vals = s.coo()
+    handle.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 1, 1e-10)
+    x = np.random.default_rng(18).random(s.n)
+    ref = sp.coo_matrix((vals, (rows, cols)), shape=(s.n, s.n)).dot(x)
+    y = handle.spmv(x)
+    assert oracle.ref_mismatches(y, ref) == 0
+    assert np.allclose(y, ref, rtol=1e-13, atol=1e-13 * np.abs(ref).max())
+
+
 def test_tuning_reused_for_same_structure(handle):
     # a new matrix (MODE_DEFAULT) with the structure of the last tuned one keeps
     # its SpMV choice without timing again; another structure is timed anew
