@@ -253,21 +253,30 @@ def test_forced_fp32_config_same_bits(handle):
 def test_pcgtest_flow_known_x(handle, case, zipf_small):
     # pcg/sw/tests/pcgtest.cpp:104-135 with pcg/sw/utils/genMat.py:38-98 data:
     # x = rand(n), b = A x, diag from the matrix; maxIter 5000, tol 1e-12
-    # (runAllPcgTests.sh); a DEFAULT solve, then KEEP_NZ_LAYOUT re-solves;
-    # each passes on zero mismatches of the reference's compare against x, or
-    # when the solve ran to maxIter
+    # (runAllPcgTests.sh); a DEFAULT solve, then KEEP_NZ_LAYOUT re-solves.
+    # pcgtest passes on zero mismatches of its compare against x, or when the
+    # solve ran to maxIter.  A residual-based stop leaves components on tiny
+    # diagonals loosely determined (the Zipf system scales rows by 10^+-3): the
+    # oracle's own solve has the same mismatches there, so the bar is no more
+    # mismatches than the oracle's, zero where the oracle has zero.
     s = {"poisson7_24": lambda: W.poisson7(24), "diffusion27_20": lambda: W.diffusion27(20, seed=15),
          "zipf_30k": lambda: zipf_small}[case]()
     rng = np.random.default_rng(16)
     x_true = rng.random(s.n)
     b = oracle.spmv(s.rowptr, s.col, s.val, x_true)
+    ref = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, b, 5000, 1e-12)
+    ref_bad = oracle.ref_mismatches(ref["x"], x_true)
+    if case != "zipf_30k":
+        assert ref_bad == 0
     rows, cols, vals = s.coo()
     for run in range(3):
         mode = X.MODE_DEFAULT if run == 0 else X.MODE_KEEP_NZ_LAYOUT
         r = handle.coo_solve(s.n, rows if run == 0 else None, cols if run == 0 else None, vals, s.diag, b,
                              5000, 1e-12, mode=mode, nnz=len(vals))
         assert r.status in (X.SUCCESS, X.EXECUTION_FAILED), r.message
-        assert oracle.ref_mismatches(r.x, x_true) == 0 or r.iters == 5000, (run, r.iters)
+        assert oracle.ref_mismatches(r.x, x_true) <= ref_bad or r.iters == 5000, (run, r.iters)
+        assert abs(r.iters - ref["iters"]) <= max(1, int(0.01 * ref["iters"]))
+        assert np.linalg.norm(r.x - ref["x"]) <= X_TOL * np.linalg.norm(ref["x"])
 
 
 def test_spmv_gen_vectors_refvec(handle):
