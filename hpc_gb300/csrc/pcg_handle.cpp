@@ -1626,11 +1626,12 @@ int PcgHandle::tuning(float* ms, int* shape, int cap) const {
             shape[4 * c + 2] = merge_items_per_thread();
             shape[4 * c + 3] = 0;
         } else if (isPat(c)) {
-            // shared-offset sliced layout: (1, 2, unroll, 0)
+            // shared-offset sliced layout: (1, 2, unroll, 1 when the values
+            // are prefetched by TMA bulk copies (FP32 only) else 0)
             shape[4 * c] = 1;
             shape[4 * c + 1] = 2;
             shape[4 * c + 2] = sellpat_config_unroll(c - patCfg0());
-            shape[4 * c + 3] = 0;
+            shape[4 * c + 3] = sellpat_config_tma(c - patCfg0());
         } else if (isSorted(c)) {
             // length-sorted sliced layout: (1, 1, unroll, 32)
             shape[4 * c] = 1;

@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "xjpcg_device.cuh"
 #include "xjpcg_internal.hpp"
@@ -259,11 +260,155 @@ __global__ void __launch_bounds__(kPatThreads, 6) spmv_sellpat_kernel(
     }
 }
 
+// TMA-fed form (FP32).  Each warp walks its slices as the plain kernel does,
+// but lane 0 prefetches the whole value block of the warp's next shared slice
+// (32 rows x its stored columns, contiguous) into shared memory with one
+// cp.async.bulk on an mbarrier while the warp computes the current slice from
+// the other buffer.  A warp thus keeps a whole slice (3.5 KB for a 27-point
+// stencil) in flight with no registers held for it.  Slices with per-entry
+// columns, or more than kTmaCols stored columns, take the plain loads.  Every
+// wait is bounded (2 s); on expiry the warp drains its other copy (bounded),
+// records kStatusWaitTimeout, marks the loop done and stops.  The FMAs run in
+// the plain kernel's order, so the sums are the same bit for bit.
+constexpr int kTmaCols = 32;
+constexpr uint64_t kTmaWaitNs = 2000000000ull;
+
+// Slice t is prefetched when it has shared offsets and fits a buffer.
+__device__ __forceinline__ bool tma_fetchable(const int* __restrict__ sliceOff, const int* __restrict__ patLen, int t,
+                                              int& off, int& len) {
+    off = __ldg(&sliceOff[t]);
+    len = (__ldg(&sliceOff[t + 1]) - off) >> 5;
+    return __ldg(&patLen[t]) > 0 && len > 0 && len <= kTmaCols;
+}
+
+template <typename VT, int U>
+__global__ void __launch_bounds__(kPatThreads, 3) spmv_sellpat_tma_kernel(
+    int n, int nslices, const int* __restrict__ sliceOff, const int* __restrict__ patLen,
+    const int* __restrict__ patIdx, const int* __restrict__ patOff, const int* __restrict__ genOff,
+    const int* __restrict__ pat, const int* __restrict__ gcol, const VT* __restrict__ sval,
+    const VT* __restrict__ x, VT* __restrict__ y, const VT* __restrict__ b, CgState* state, double* partials,
+    int mode, const uint32_t* doneFlag) {
+    typedef typename PatAcc<VT>::type AccT;
+    extern __shared__ __align__(128) unsigned char tmaSmem[];
+    __shared__ __align__(8) uint64_t bars[kPatThreads / 32][2];
+    if (doneFlag && *(volatile const uint32_t*)doneFlag) return;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
+    VT* bufs = reinterpret_cast<VT*>(tmaSmem) + (size_t)wid * 2 * kTmaCols * 32;
+    if (lane == 0) {
+        mbar_init(&bars[wid][0], 1);
+        mbar_init(&bars[wid][1], 1);
+        mbar_fence_init();
+    }
+    __syncwarp();
+    const uint64_t pol = l2_policy_evict_first();
+    uint32_t phase0 = 0u, phase1 = 0u;  // parity of each buffer's next completion
+    bool abort = false;
+    AccT dacc = AccT(0);
+    int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int off = 0, len = 0;
+    bool fits = s < nslices && tma_fetchable(sliceOff, patLen, s, off, len);
+    if (fits && lane == 0) {
+        const uint32_t bytes = (uint32_t)(len * 32 * sizeof(VT));
+        mbar_arrive_expect_tx(&bars[wid][0], bytes);
+        bulk_g2s(bufs, sval + off, bytes, &bars[wid][0], pol);
+    }
+    for (int k = 0; s < nslices; s += warpsPerGrid, ++k) {
+        const int cb = k & 1;
+        VT* cur = bufs + cb * kTmaCols * 32;
+        VT* nxt = bufs + (cb ^ 1) * kTmaCols * 32;
+        const int sn = s + warpsPerGrid;
+        int offn = 0, lenn = 0;
+        const bool fitsn = sn < nslices && tma_fetchable(sliceOff, patLen, sn, offn, lenn);
+        if (fitsn && lane == 0) {
+            const uint32_t bytes = (uint32_t)(lenn * 32 * sizeof(VT));
+            mbar_arrive_expect_tx(&bars[wid][cb ^ 1], bytes);
+            bulk_g2s(nxt, sval + offn, bytes, &bars[wid][cb ^ 1], pol);
+        }
+        const int row = s * 32 + lane;
+        AccT acc = AccT(0);
+        if (fits) {
+            const uint32_t ph = cb ? phase1 : phase0;
+            const bool ok = mbar_wait_bounded(&bars[wid][cb], ph, kTmaWaitNs);
+            if (cb)
+                phase1 ^= 1u;
+            else
+                phase0 ^= 1u;
+            if (__any_sync(0xffffffffu, !ok)) {
+                abort = true;
+                if (fitsn) mbar_wait_bounded(&bars[wid][cb ^ 1], cb ? phase0 : phase1, kTmaWaitNs);  // drain
+                break;
+            }
+            const int* p = pat + __ldg(&patOff[__ldg(&patIdx[s])]);
+            const VT* xr = x + row;
+            int j = 0;
+            for (; j + U <= len; j += U) {
+                VT v[U];
+                int o[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    v[u] = cur[(j + u) * 32 + lane];
+                    o[u] = __ldg(p + j + u);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) acc = fma((AccT)v[u], (AccT)__ldg(xr + o[u]), acc);
+            }
+            for (; j < len; ++j) acc = fma((AccT)cur[j * 32 + lane], (AccT)__ldg(xr + __ldg(p + j)), acc);
+        } else {
+            const int offp = __ldg(&sliceOff[s]);
+            const int lenp = (__ldg(&sliceOff[s + 1]) - offp) >> 5;
+            const VT* vp = sval + offp + lane;
+            if (__ldg(&patLen[s]) > 0) {
+                const int* p = pat + __ldg(&patOff[__ldg(&patIdx[s])]);
+                const VT* xr = x + row;
+                for (int j = 0; j < lenp; ++j) acc = fma((AccT)__ldcs(vp + j * 32), (AccT)__ldg(xr + __ldg(p + j)), acc);
+            } else {
+                const int* cp = gcol + __ldg(&genOff[s]) + lane;
+                for (int j = 0; j < lenp; ++j)
+                    acc = fma((AccT)__ldcs(vp + j * 32), (AccT)__ldg(&x[__ldcs(cp + j * 32)]), acc);
+            }
+        }
+        if (row < n) {
+            if (mode == kSpmvResidual) {
+                const AccT rv = (AccT)b[row] - acc;
+                y[row] = (VT)rv;
+                dacc = fma(rv, rv, dacc);
+            } else {
+                y[row] = (VT)acc;
+                if (mode == kSpmvCgDot) dacc = fma((AccT)x[row], acc, dacc);
+            }
+        }
+        __syncwarp();  // every lane is done with cur before it is refilled
+        fits = fitsn;
+        off = offn;
+        len = lenn;
+    }
+    if (abort && lane == 0) {
+        atomicOr(&state->status, kStatusWaitTimeout);
+        *(volatile uint32_t*)&state->done = 1u;  // later kernels of the loop stand down
+    }
+    if (mode == kSpmvPlain) return;
+    AccT v[1] = {dacc};
+    block_sum<kPatThreads, 1, AccT>(v);
+    double tot[1] = {(double)v[0]}, fin[1];
+    if (grid_sum_last<kPatThreads, 1>(tot, partials, &state->counters[0], fin)) {
+        if (threadIdx.x == 0) {
+            if (mode == kSpmvCgDot) {
+                state->pAp = fin[0];
+                state->alpha = state->rz / fin[0];
+            } else {
+                state->rrTrue = fin[0];
+            }
+        }
+    }
+}
+
 // ---- host side ----
 // Unroll 4 and 8 (an unroll-16 build at 64 registers measured slower in
-// both precisions).
-int sellpat_num_configs() { return 2; }
-int sellpat_config_unroll(int cfg) { return cfg == 0 ? 4 : 8; }
+// both precisions), then, FP32 only, the TMA-fed unroll 4 and 8.
+int sellpat_num_configs() { return 4; }
+int sellpat_config_unroll(int cfg) { return (cfg & 1) ? 8 : 4; }
+int sellpat_config_tma(int cfg) { return cfg >= 2 ? 1 : 0; }
 
 // Plans the layout.  Per slice (nslices + 1 ints each): sliceOff (values),
 // patLen, patNew, patIdx (before sellpat_index: the scan of patNew), genOff.
@@ -345,11 +490,55 @@ int sp_bps() {
         return 0;
     return nb;
 }
+
+constexpr size_t kTmaSmem = (size_t)(kPatThreads / 32) * 2 * kTmaCols * 32 * sizeof(float);
+
+template <int U>
+int sp_tma_bps() {
+    int nb = 0;
+    if (cudaFuncSetAttribute(spmv_sellpat_tma_kernel<float, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kTmaSmem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_sellpat_tma_kernel<float, U>, kPatThreads,
+                                                      kTmaSmem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nb;
+}
+
+template <typename VT>
+int sp_config_bps(int cfg) {
+    if (cfg == 0) return sp_bps<VT, 4>();
+    if (cfg == 1) return sp_bps<VT, 8>();
+    if (!std::is_same<VT, float>::value) return 0;  // the TMA-fed forms are FP32 only
+    if (cfg == 2) return sp_tma_bps<4>();
+    if (cfg == 3) return sp_tma_bps<8>();
+    return 0;
+}
+
+template <typename VT>
+struct PatTma {
+    template <typename... A>
+    static cudaError_t launch(int, int, cudaStream_t, A...) {
+        return cudaErrorInvalidValue;
+    }
+};
+template <>
+struct PatTma<float> {
+    template <typename... A>
+    static cudaError_t launch(int cfg, int grid, cudaStream_t st, A... args) {
+        if (cfg == 2)
+            spmv_sellpat_tma_kernel<float, 4><<<grid, kPatThreads, kTmaSmem, st>>>(args...);
+        else
+            spmv_sellpat_tma_kernel<float, 8><<<grid, kPatThreads, kTmaSmem, st>>>(args...);
+        return cudaGetLastError();
+    }
+};
 }  // namespace
 
 template <typename VT>
 int sellpat_grid(int cfg, int n, int numSms) {
-    const int bps = sellpat_config_unroll(cfg) == 4 ? sp_bps<VT, 4>() : sp_bps<VT, 8>();
+    const int bps = sp_config_bps<VT>(cfg);
     if (bps <= 0) return 0;
     const int nslices = (n + 31) / 32;
     const int need = (nslices + kPatThreads / 32 - 1) / (kPatThreads / 32);
@@ -363,6 +552,9 @@ cudaError_t spmv_sellpat_launch(int cfg, int grid, cudaStream_t st, int n, const
                                 double* partials, int mode, const uint32_t* doneFlag) {
     if (n <= 0) return cudaSuccess;
     const int nslices = (n + 31) / 32;
+    if (sellpat_config_tma(cfg))
+        return PatTma<VT>::launch(cfg, grid, st, n, nslices, sliceOff, patLen, patIdx, patOff, genOff, pat, gcol,
+                                  sval, x, y, b, state, partials, mode, doneFlag);
     if (sellpat_config_unroll(cfg) == 4)
         spmv_sellpat_kernel<VT, 4><<<grid, kPatThreads, 0, st>>>(n, nslices, sliceOff, patLen, patIdx, patOff,
                                                                  genOff, pat, gcol, sval, x, y, b, state, partials,

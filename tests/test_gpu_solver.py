@@ -228,21 +228,26 @@ def test_every_forced_config(handle, zipf_small):
         handle.set_spmv_config(-1)
 
 
-def test_forced_fp32_config_same_bits(handle):
-    # the mixed solver's FP32 SpMV forced to each shared-offset form: the
-    # unroll does not change the order of a row's FMAs, so the mixed solves
-    # agree bit for bit; a configuration index out of range is refused
-    s = W.diffusion27(30, seed=14)
+@pytest.mark.parametrize("nx", [30, 41])
+def test_forced_fp32_config_same_bits(handle, nx):
+    # the mixed solver's FP32 SpMV forced to each shared-offset form (unroll
+    # 4 and 8, plain loads or TMA-fed values): none changes the order of a
+    # row's FMAs, so the mixed solves agree bit for bit; the TMA-fed forms are
+    # FP32 only; a configuration index out of range is refused
+    s = W.diffusion27(nx, seed=14)
     handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
     shapes = [t[:4] for t in handle.spmv_tuning()]
-    cfgs = [shapes.index((1, 2, u, 0)) for u in (4, 8)]
+    cfgs = [shapes.index((1, 2, u, t)) for t in (0, 1) for u in (4, 8)]
+    with pytest.raises(X.XJPCGError):
+        handle.set_spmv_config(cfgs[2])
     out = []
     for c in cfgs:
         handle.set_spmv_config32(c)
         m = handle.mixed_solve(s.b, s.diag, 20000, 1e-10)
         assert m.status == X.SUCCESS and handle.info().spmvCfg32 == c
         out.append((m.iters, m.x.copy()))
-    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
+    for it, xs in out[1:]:
+        assert it == out[0][0] and np.array_equal(xs, out[0][1])
     assert oracle.true_relres(s.rowptr, s.col, s.val, s.b, out[0][1]) <= RES_TOL * 1.5
     with pytest.raises(X.XJPCGError):
         handle.set_spmv_config32(len(shapes))
