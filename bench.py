@@ -72,6 +72,36 @@ def dist_env():
     return rank, world, local
 
 
+class Ranks:
+    """The timing protocol across ranks: a barrier on both sides of the timed
+    region and the maximum of the per-rank times.  The GPU arm runs it over
+    NCCL with CUDA tensors; with a gloo group it uses CPU tensors."""
+
+    def __init__(self, world: int, device: str):
+        self.world = world
+        self.device = device
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+def replicas_value(world: int, steps: int, t_max: float) -> float:
+    """Whole-job throughput of independent replicas: every rank ran `steps`
+    steps, the slowest in t_max seconds."""
+    return world * steps / t_max
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -377,16 +407,8 @@ def run_gb300(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
-    def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    ranks = Ranks(world, "cuda")
+    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     sysm = W.diffusion27(args.nx)
     n, nnz = sysm.n, sysm.nnz
@@ -442,7 +464,7 @@ def run_gb300(args):
     t = ev0.elapsed_time(ev1) / 1e3
     t = max_over_ranks(t)
     ttt = t / args.steps
-    value = world * args.steps / t
+    value = replicas_value(world, args.steps, t)
     k_iters = int(np.median(iters))
     launches = sum(1 + 3 * k for k in iters)
 
@@ -486,7 +508,7 @@ def run_gb300(args):
         torch.cuda.synchronize()
         te = max_over_ranks(time.perf_counter() - t0)
         met, inf_e = h.metrics(), h.info()
-        e2e = {"value": world * args.steps / te, "unit": "solves/s",
+        e2e = {"value": replicas_value(world, args.steps, te), "unit": "solves/s",
                "h2d_bytes_per_step": int(4 * nnz + 4 * nnz + 8 * nnz + 8 * n + 8 * n),
                "d2h_bytes_per_step": int(8 * n + 256), "time_to_tol_s": te / args.steps,
                "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays", "step_s": step_s,
