@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(NT) batched_fp64_kernel(BatchArgs a) {
 
 // Mixed precision with reliable updates, per system (the batched form of
 // mixed_kernels.cu): the CG recurrences run in FP32 (values, r, p, Ap, J and
-// the increment d; per-thread sums in FP32, CTA sums in FP64) and keep their
+// the increment d; per-thread and CTA sums in FP32) and keep their
 // search direction.  When the FP32 residual norm has fallen by delta below its
 // largest value since the last refresh, looks converged, or the budget is
 // spent, the refresh folds d into the FP64 x, recomputes r = b - A x with the
@@ -294,9 +294,12 @@ __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
                     pAp = fmaf(P[row], acc, pAp);
                 }
             }
-            double v1[1] = {(double)pAp};
-            block_allreduce<NT, 1, double>(v1);
-            const double alphaD = rz / v1[0];
+            // The inner solve's CTA sums run in FP32 like its per-thread sums:
+            // in double they cost FP64 adds in every warp, which on this part
+            // held the FP64 pipe 30 % busy in a kernel that is otherwise FP32.
+            float v1[1] = {pAp};
+            block_allreduce<NT, 1, float>(v1);
+            const double alphaD = rz / (double)v1[0];
             const float alpha = (float)alphaD;
             float rrP = 0.f, rzP = 0.f;
             for (int i = tid; i < n; i += NT) {
@@ -308,8 +311,8 @@ __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
                 rrP = fmaf(ri, ri, rrP);
                 rzP = fmaf(ri, zi, rzP);
             }
-            double w[2] = {(double)rrP, (double)rzP};
-            block_allreduce<NT, 2, double>(w);
+            float w[2] = {rrP, rzP};
+            block_allreduce<NT, 2, float>(w);
             ++k;
             const double rrN = w[0], rzN = w[1];
             if (rrN > rrMax) rrMax = rrN;
