@@ -64,13 +64,18 @@ struct BatchArgs {
     int smemRows;      // p capacity in shared memory (rows)
 };
 
-// CTA sum returned in every thread: a shuffle tree in every warp, then one
-// over the warp totals.  Here it measured faster than the narrow
-// block_allsum (176 against 190 ms for 4,096 systems in fp64): with it the
-// compiler keeps the chosen 512-thread shape at three CTAs per SM without
-// spills, and the many resident CTAs hide the tree's extra FP64 adds.
+// CTA sum returned in every thread.  Doubles: the narrow block_allsum, in
+// which warp 0 alone adds the threads' values in a fixed order
+// (xjpcg_device.cuh), so few FP64 adds are spent.  The FP64 kernel pins three
+// 512-thread CTAs per SM (1,536 threads) in its launch bounds: left to the
+// compiler, the narrow sum's lower register count moved it to four CTAs with
+// spills, which measured slower than a shuffle tree (190 against 176 ms for
+// 4,096 systems); pinned, it measures 172 ms.  Floats (the mixed kernel's
+// inner sums): a shuffle tree in every warp, which costs no FP64 work and
+// keeps the serial chain of warp 0 off the critical path (111.5 ms against
+// 122.5 ms with the narrow form).
 template <int NT, int NV, typename T>
-__device__ __forceinline__ void block_allreduce(T (&v)[NV]) {
+__device__ __forceinline__ void block_allreduce_tree(T (&v)[NV]) {
     __shared__ T red[NV][NT / 32];
     __shared__ T bc[NV];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -93,6 +98,14 @@ __device__ __forceinline__ void block_allreduce(T (&v)[NV]) {
 #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = bc[i];
     __syncthreads();
+}
+
+template <int NT, int NV, typename T>
+__device__ __forceinline__ void block_allreduce(T (&v)[NV]) {
+    if (std::is_same<T, float>::value)
+        block_allreduce_tree<NT, NV, T>(v);
+    else
+        block_allsum<NT, NV, T>(v);
 }
 
 // CG on one system: A d = rhs, d0 = 0, Jacobi preconditioner J.  On entry r
@@ -190,7 +203,7 @@ __device__ __forceinline__ int next_system(const BatchArgs& a) {
 }
 
 template <int NT, int G>
-__global__ void __launch_bounds__(NT) batched_fp64_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_fp64_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     double* pS = reinterpret_cast<double*>(smem);
     for (;;) {
