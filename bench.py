@@ -337,6 +337,7 @@ def batched_measure(X, count=4096):
                     "converged": int(np.sum((res["status"] == 0) & (res["res"] <= 1e-10))),
                     "iters_total": int(res["itersRun"].sum()), "threads": inf.batchThreads,
                     "lanes": inf.batchLanes, "smem_rows": inf.batchSmemRows, "grid": inf.batchGrid,
+                    "sliced": bool(inf.batchSliced),
                     "max_err_vs_oracle_sample": err,
                     "oracle": "oracle JPCG to 1e-14 (FP64, CPU) on %d sampled systems" % len(sample)}
     h.close()

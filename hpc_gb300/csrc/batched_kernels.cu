@@ -62,7 +62,39 @@ struct BatchArgs {
     double tol;
     double delta2;     // mixed: refresh when the FP32 r.r falls below delta2 * its running maximum
     int smemRows;      // p capacity in shared memory (rows)
+    // per-system SELL-32 copy (sliced kernels): slice s of system i is global
+    // slice sliceBase[i] + s; its 32 x width stored entries start at
+    // sliceOff[global slice], slice-column-major, with 16-bit local columns
+    const int* sliceBase;
+    const int* sliceOff;
+    const double* sval;
+    const float* sval32;
+    const uint16_t* scol;
 };
+
+// One sliced row sum: lane l of the warp holds row 32 j + l of its system.
+template <typename VT, typename AccT>
+__device__ __forceinline__ AccT slice_dot(const int* __restrict__ sliceOff, int j, const VT* __restrict__ sval,
+                                          const uint16_t* __restrict__ scol, const VT* P, int lane32) {
+    const int off = sliceOff[j], w = (sliceOff[j + 1] - off) >> 5;
+    const VT* vp = sval + off + lane32;
+    const uint16_t* cp = scol + off + lane32;
+    AccT acc = AccT(0);
+    int k = 0;
+    for (; k + 4 <= w; k += 4) {
+        VT v[4];
+        int c[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[u] = __ldcs(vp + 32 * (k + u));
+            c[u] = __ldcs(cp + 32 * (k + u));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc = fma((AccT)v[u], (AccT)P[c[u]], acc);
+    }
+    for (; k < w; ++k) acc = fma((AccT)__ldcs(vp + 32 * k), (AccT)P[__ldcs(cp + 32 * k)], acc);
+    return acc;
+}
 
 // CTA sum returned in every thread.  Doubles: the narrow block_allsum, in
 // which warp 0 alone adds the threads' values in a fixed order
@@ -113,11 +145,12 @@ __device__ __forceinline__ void block_allreduce(T (&v)[NV]) {
 // the vectors and matrix values; reductions leave the CTA in double.
 // Stop: rr < tols (tols = rr0 * relTol^2) or k reaches maxK.  Returns k (the
 // iterations run) and the last r.r / rr0 through the references.
-template <typename VT, int NT, int G>
+template <typename VT, int NT, int G, bool SL>
 __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const int* __restrict__ col,
-                            const VT* __restrict__ val, VT* __restrict__ r, VT* __restrict__ d,
-                            const VT* __restrict__ J, VT* __restrict__ Ap, VT* P, double relTol, uint32_t maxK,
-                            double& rrLast, double& rr0Out, bool& breakdown) {
+                            const VT* __restrict__ val, const int* __restrict__ sliceOff,
+                            const VT* __restrict__ sval, const uint16_t* __restrict__ scol, VT* __restrict__ r,
+                            VT* __restrict__ d, const VT* __restrict__ J, VT* __restrict__ Ap, VT* P, double relTol,
+                            uint32_t maxK, double& rrLast, double& rr0Out, bool& breakdown) {
     typedef typename std::conditional<sizeof(VT) == 8, double, float>::type AccT;
     const int tid = threadIdx.x;
     AccT rzA = 0, rrA = 0;
@@ -142,21 +175,33 @@ __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const
     for (;;) {
         // Ap = A p, p.Ap
         AccT pAp = 0;
-        // Row blocks are warp-uniform so the lane shuffles always see 32 lanes.
-        for (int rb = (tid >> 5) * (32 / G); rb < n; rb += NT / G) {
-            const int row = rb + (tid & 31) / G;
-            AccT acc = 0;
-            if (row < n) {
-                const int s = rowptr[row] - e0, e = rowptr[row + 1] - e0;
-                for (int q = s + lane; q < e; q += G) acc = fma((AccT)val[q], (AccT)P[col[q]], acc);
+        if (SL) {
+            // warp w takes slices w, w + NT/32, ...: 32 rows, one per lane
+            for (int j = tid >> 5; 32 * j < n; j += NT / 32) {
+                const AccT acc = slice_dot<VT, AccT>(sliceOff, j, sval, scol, P, tid & 31);
+                const int row = 32 * j + (tid & 31);
+                if (row < n) {
+                    Ap[row] = (VT)acc;
+                    pAp = fma((AccT)P[row], acc, pAp);
+                }
             }
-            if (G > 1) {
+        } else {
+            // Row blocks are warp-uniform so the lane shuffles always see 32 lanes.
+            for (int rb = (tid >> 5) * (32 / G); rb < n; rb += NT / G) {
+                const int row = rb + (tid & 31) / G;
+                AccT acc = 0;
+                if (row < n) {
+                    const int s = rowptr[row] - e0, e = rowptr[row + 1] - e0;
+                    for (int q = s + lane; q < e; q += G) acc = fma((AccT)val[q], (AccT)P[col[q]], acc);
+                }
+                if (G > 1) {
 #pragma unroll
-                for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
-            }
-            if (lane == 0 && row < n) {
-                Ap[row] = (VT)acc;
-                pAp = fma((AccT)P[row], acc, pAp);
+                    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+                }
+                if (lane == 0 && row < n) {
+                    Ap[row] = (VT)acc;
+                    pAp = fma((AccT)P[row], acc, pAp);
+                }
             }
         }
         double v1[1] = {(double)pAp};
@@ -202,7 +247,7 @@ __device__ __forceinline__ int next_system(const BatchArgs& a) {
     return t < a.nsys ? a.order[t] : -1;
 }
 
-template <int NT, int G>
+template <int NT, int G, bool SL>
 __global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_fp64_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     double* pS = reinterpret_cast<double*>(smem);
@@ -223,8 +268,9 @@ __global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_f
         __syncthreads();
         double rrLast, rr0;
         bool bd;
-        const uint32_t k = cg_core<double, NT, G>(n, a.rowptr + r0, e0, a.col + e0, a.val + e0, a.r + r0, a.x + r0,
-                                                  a.J + r0, a.Ap + r0, P, a.tol, a.maxIterP1, rrLast, rr0, bd);
+        const uint32_t k = cg_core<double, NT, G, SL>(
+            n, a.rowptr + r0, e0, a.col + e0, a.val + e0, SL ? a.sliceOff + a.sliceBase[sys] : nullptr, a.sval, a.scol,
+            a.r + r0, a.x + r0, a.J + r0, a.Ap + r0, P, a.tol, a.maxIterP1, rrLast, rr0, bd);
         if (threadIdx.x == 0) {
             BatchResult& o = a.res[sys];
             o.itersRun = k;
@@ -245,7 +291,7 @@ __global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_f
 // spent, the refresh folds d into the FP64 x, recomputes r = b - A x with the
 // FP64 matrix and restarts the FP32 residual from it.  The system stops on the
 // true FP64 residual: r.r <= b.b tol^2.
-template <int NT, int G>
+template <int NT, int G, bool SL>
 __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* pS = reinterpret_cast<float*>(smem);
@@ -291,25 +337,34 @@ __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
         while (!stop) {
             // Ap = A p (FP32), p.Ap
             float pAp = 0.f;
-            for (int rb = (tid >> 5) * (32 / G); rb < n; rb += NT / G) {
-                const int row = rb + (tid & 31) / G;
-                float acc = 0.f;
-                if (row < n) {
-                    const int s0 = rp[row] - e0, s1 = rp[row + 1] - e0;
-                    for (int q = s0 + lane; q < s1; q += G) acc = fmaf(vl32[q], P[cl[q]], acc);
+            if (SL) {
+                const int* so = a.sliceOff + a.sliceBase[sys];
+                for (int j = tid >> 5; 32 * j < n; j += NT / 32) {
+                    const float acc = slice_dot<float, float>(so, j, a.sval32, a.scol, P, tid & 31);
+                    const int row = 32 * j + (tid & 31);
+                    if (row < n) {
+                        Ap[row] = acc;
+                        pAp = fmaf(P[row], acc, pAp);
+                    }
                 }
-                if (G > 1) {
+            } else {
+                for (int rb = (tid >> 5) * (32 / G); rb < n; rb += NT / G) {
+                    const int row = rb + (tid & 31) / G;
+                    float acc = 0.f;
+                    if (row < n) {
+                        const int s0 = rp[row] - e0, s1 = rp[row + 1] - e0;
+                        for (int q = s0 + lane; q < s1; q += G) acc = fmaf(vl32[q], P[cl[q]], acc);
+                    }
+                    if (G > 1) {
 #pragma unroll
-                    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
-                }
-                if (lane == 0 && row < n) {
-                    Ap[row] = acc;
-                    pAp = fmaf(P[row], acc, pAp);
+                        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+                    }
+                    if (lane == 0 && row < n) {
+                        Ap[row] = acc;
+                        pAp = fmaf(P[row], acc, pAp);
+                    }
                 }
             }
-            // The inner solve's CTA sums run in FP32 like its per-thread sums:
-            // in double they cost FP64 adds in every warp, which on this part
-            // held the FP64 pipe 30 % busy in a kernel that is otherwise FP32.
             float v1[1] = {pAp};
             block_allreduce<NT, 1, float>(v1);
             const double alphaD = rz / (double)v1[0];
@@ -390,19 +445,20 @@ __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
 
 // ---------------------------------------------------------------------------
 namespace {
-template <int NT, int G>
+template <int NT, int G, bool SL>
 struct BatchInst {
     static cudaError_t launch(bool mixed, int grid, size_t smem, cudaStream_t st, const BatchArgs& a) {
+        if (SL && a.sliceOff == nullptr) return cudaErrorInvalidValue;  // no sliced copy
         if (mixed) {
-            cudaError_t e = cudaFuncSetAttribute(batched_mixed_kernel<NT, G>,
+            cudaError_t e = cudaFuncSetAttribute(batched_mixed_kernel<NT, G, SL>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
-            batched_mixed_kernel<NT, G><<<grid, NT, smem, st>>>(a);
+            batched_mixed_kernel<NT, G, SL><<<grid, NT, smem, st>>>(a);
         } else {
-            cudaError_t e = cudaFuncSetAttribute(batched_fp64_kernel<NT, G>,
+            cudaError_t e = cudaFuncSetAttribute(batched_fp64_kernel<NT, G, SL>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
-            batched_fp64_kernel<NT, G><<<grid, NT, smem, st>>>(a);
+            batched_fp64_kernel<NT, G, SL><<<grid, NT, smem, st>>>(a);
         }
         return cudaGetLastError();
     }
@@ -410,11 +466,13 @@ struct BatchInst {
         int nb = 0;
         cudaError_t e;
         if (mixed) {
-            cudaFuncSetAttribute(batched_mixed_kernel<NT, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_mixed_kernel<NT, G>, NT, smem);
+            cudaFuncSetAttribute(batched_mixed_kernel<NT, G, SL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_mixed_kernel<NT, G, SL>, NT, smem);
         } else {
-            cudaFuncSetAttribute(batched_fp64_kernel<NT, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_fp64_kernel<NT, G>, NT, smem);
+            cudaFuncSetAttribute(batched_fp64_kernel<NT, G, SL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_fp64_kernel<NT, G, SL>, NT, smem);
         }
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -426,17 +484,19 @@ struct BatchInst {
 
 struct BatchCfg {
     int threads, lanes;
+    bool sliced;
     cudaError_t (*launch)(bool, int, size_t, cudaStream_t, const BatchArgs&);
     int (*bps)(bool, size_t);
 };
+#define XJ_BATCH_CFG(NTV, GV, SLV) \
+    { NTV, GV, SLV, &BatchInst<NTV, GV, SLV>::launch, &BatchInst<NTV, GV, SLV>::blocksPerSm }
+// CSR kernels (threads x lanes per row), then the sliced kernels (one lane per row)
 const BatchCfg kBatchCfgs[] = {
-    {256, 1, &BatchInst<256, 1>::launch, &BatchInst<256, 1>::blocksPerSm},
-    {256, 2, &BatchInst<256, 2>::launch, &BatchInst<256, 2>::blocksPerSm},
-    {512, 1, &BatchInst<512, 1>::launch, &BatchInst<512, 1>::blocksPerSm},
-    {512, 2, &BatchInst<512, 2>::launch, &BatchInst<512, 2>::blocksPerSm},
-    {128, 1, &BatchInst<128, 1>::launch, &BatchInst<128, 1>::blocksPerSm},
-    {1024, 1, &BatchInst<1024, 1>::launch, &BatchInst<1024, 1>::blocksPerSm},
+    XJ_BATCH_CFG(256, 1, false), XJ_BATCH_CFG(256, 2, false), XJ_BATCH_CFG(512, 1, false),
+    XJ_BATCH_CFG(512, 2, false), XJ_BATCH_CFG(128, 1, false), XJ_BATCH_CFG(1024, 1, false),
+    XJ_BATCH_CFG(256, 1, true),  XJ_BATCH_CFG(512, 1, true),  XJ_BATCH_CFG(1024, 1, true),
 };
+#undef XJ_BATCH_CFG
 }  // namespace
 
 __global__ void batch_validate_kernel(int nsys, const int* __restrict__ sysRow, const int* __restrict__ rowptr,
@@ -469,6 +529,91 @@ void batch_config_shape(int cfg, int* threads, int* lanes) {
     *threads = kBatchCfgs[cfg].threads;
     *lanes = kBatchCfgs[cfg].lanes;
 }
+bool batch_config_sliced(int cfg) { return kBatchCfgs[cfg].sliced; }
+
+// ---- per-system SELL-32 copy ----
+namespace {
+__device__ __forceinline__ int warp_max_i(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// System of global slice g: the largest s with sliceBase[s] <= g.
+__device__ __forceinline__ int system_of_slice(const int* __restrict__ sliceBase, int nsys, int g) {
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sliceBase[mid] <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+}  // namespace
+
+// One warp per slice: stored entries 32 x (the slice's longest row).
+__global__ void bsell_width_kernel(int nsys, int nslices, const int* __restrict__ sysRow,
+                                   const int* __restrict__ sliceBase, const int* __restrict__ rowptr,
+                                   int* __restrict__ len) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nslices; g += warps) {
+        const int s = system_of_slice(sliceBase, nsys, g);
+        const int r0 = sysRow[s], n = sysRow[s + 1] - r0;
+        const int lr = (g - sliceBase[s]) * 32 + lane;
+        const int rl = lr < n ? rowptr[r0 + lr + 1] - rowptr[r0 + lr] : 0;
+        const int w = warp_max_i(rl);
+        if (lane == 0) len[g] = 32 * w;
+    }
+}
+
+// One warp per slice: values (and, when scol is given, local columns) in
+// slice-column-major order; padding entries hold value 0 and column 0.
+template <typename VT>
+__global__ void bsell_fill_kernel(int nsys, int nslices, const int* __restrict__ sysRow,
+                                  const int* __restrict__ sliceBase, const int* __restrict__ rowptr,
+                                  const int* __restrict__ col, const double* __restrict__ val,
+                                  const int* __restrict__ sliceOff, VT* __restrict__ sval, uint16_t* __restrict__ scol) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nslices; g += warps) {
+        const int s = system_of_slice(sliceBase, nsys, g);
+        const int r0 = sysRow[s], n = sysRow[s + 1] - r0;
+        const int lr = (g - sliceBase[s]) * 32 + lane;
+        const int j0 = lr < n ? rowptr[r0 + lr] : 0, j1 = lr < n ? rowptr[r0 + lr + 1] : 0;
+        const int off = sliceOff[g], w = (sliceOff[g + 1] - off) >> 5;
+        for (int k = 0; k < w; ++k) {
+            const bool has = j0 + k < j1;
+            sval[off + 32 * k + lane] = has ? (VT)val[j0 + k] : VT(0);
+            if (scol) scol[off + 32 * k + lane] = has ? (uint16_t)col[j0 + k] : (uint16_t)0;
+        }
+    }
+}
+
+cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
+                              const int* rowptr, int* sliceLen, int* sliceOff, int* blockSums) {
+    const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, 152 * 32));
+    bsell_width_kernel<<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, sliceLen);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return scan_exclusive(st, sliceLen, sliceOff, nslices + 1, blockSums);
+}
+
+template <typename VT>
+cudaError_t batch_sell_fill(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
+                            const int* rowptr, const int* col, const double* val, const int* sliceOff, VT* sval,
+                            uint16_t* scol) {
+    const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, 152 * 32));
+    bsell_fill_kernel<VT><<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, col, val, sliceOff, sval,
+                                                scol);
+    return cudaGetLastError();
+}
+template cudaError_t batch_sell_fill<double>(cudaStream_t, int, int, const int*, const int*, const int*, const int*,
+                                             const double*, const int*, double*, uint16_t*);
+template cudaError_t batch_sell_fill<float>(cudaStream_t, int, int, const int*, const int*, const int*, const int*,
+                                            const double*, const int*, float*, uint16_t*);
 
 // smemRows: rows of p kept in shared memory; systems larger than that keep p
 // in the global scratch vector (still correct, slower).
@@ -500,6 +645,11 @@ cudaError_t batch_launch(int cfg, bool mixed, int numSms, int smemRows, cudaStre
     a.tol = L.tol;
     a.delta2 = L.delta2;
     a.smemRows = smemRows;
+    a.sliceBase = L.sliceBase;
+    a.sliceOff = L.sliceOff;
+    a.sval = L.sval;
+    a.sval32 = L.sval32;
+    a.scol = L.scol;
     const size_t smem = (size_t)smemRows * (mixed ? sizeof(float) : sizeof(double));
     const BatchCfg& c = kBatchCfgs[cfg];
     const int bps = c.bps(mixed, smem);

@@ -1418,8 +1418,11 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
                      onDevice ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost),
           "row pointers");
     if (hRp[0] != 0) throw InvalidValue("row pointers must start at 0.");
-    for (int i = 0; i < total; ++i)
+    int maxRowLen = 0;
+    for (int i = 0; i < total; ++i) {
         if (hRp[i + 1] < hRp[i]) throw InvalidValue("row pointers are not monotone.");
+        maxRowLen = std::max(maxRowLen, hRp[i + 1] - hRp[i]);
+    }
     const int64_t nnz = hRp[total];
     // Queue order: largest systems first so the long solves start early.
     std::vector<int32_t> order(nsys);
@@ -1460,6 +1463,48 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
     if (bad) throw InvalidValue("a column index lies outside its system.");
     if (mixed) check(convert_f64_to_f32(m_stream, nnz, m_bVal.as<double>(), m_bVal32.as<float>()), "fp32 values");
 
+    // Per-system SELL-32 copy for the sliced kernels: 32-row slices of each
+    // system, values slice-column-major, 16-bit local columns.  Offered when
+    // every system has at most 65,536 rows and the copy fits 32-bit offsets.
+    int64_t nslices = 0;
+    for (uint32_t s = 0; s < nsys; ++s) nslices += (hSys[s + 1] - hSys[s] + 31) / 32;
+    const bool sliced = maxN <= 65536 && nslices * 32 * (int64_t)std::max(maxRowLen, 1) < 0x7fffff00ll &&
+                        envInt("XJPCG_BATCH_SLICED", 1) != 0;
+    if (sliced) {
+        const int nsl = (int)nslices;
+        std::vector<int32_t> hBase(nsys + 1, 0);
+        for (uint32_t s = 0; s < nsys; ++s) hBase[s + 1] = hBase[s] + (hSys[s + 1] - hSys[s] + 31) / 32;
+        alloc(m_bsBase, sizeof(int32_t) * (nsys + 1), "batch slice bases");
+        alloc(m_bsLen, sizeof(int32_t) * ((size_t)nsl + 1), "batch slice lengths");
+        alloc(m_bsOff, sizeof(int32_t) * ((size_t)nsl + 1), "batch slice offsets");
+        alloc(m_bsScan, sizeof(int32_t) * ((size_t)scan_block_count(nsl + 1) + 1), "scan scratch");
+        check(cudaMemcpyAsync(m_bsBase.p, hBase.data(), sizeof(int32_t) * (nsys + 1), cudaMemcpyHostToDevice,
+                              m_stream),
+              "H2D");
+        check(cudaMemsetAsync(m_bsLen.p, 0, sizeof(int32_t) * ((size_t)nsl + 1), m_stream), "memset");
+        check(batch_sell_widths(m_stream, (int)nsys, nsl, m_bSysRow.as<int>(), m_bsBase.as<int>(),
+                                m_bRowptr.as<int>(), m_bsLen.as<int>(), m_bsOff.as<int>(), m_bsScan.as<int>()),
+              "batch slices");
+        int stored = 0;
+        check(cudaMemcpyAsync(&stored, m_bsOff.as<int>() + nsl, sizeof(int), cudaMemcpyDeviceToHost, m_stream),
+              "D2H");
+        check(cudaStreamSynchronize(m_stream), "sync");
+        alloc(m_bsCol, sizeof(uint16_t) * ((size_t)stored + 64), "batch sliced columns");
+        if (mixed) {
+            alloc(m_bsVal32, sizeof(float) * ((size_t)stored + 32), "batch sliced fp32 values");
+            check(batch_sell_fill<float>(m_stream, (int)nsys, nsl, m_bSysRow.as<int>(), m_bsBase.as<int>(),
+                                         m_bRowptr.as<int>(), m_bCol.as<int>(), m_bVal.as<double>(), m_bsOff.as<int>(),
+                                         m_bsVal32.as<float>(), m_bsCol.as<uint16_t>()),
+                  "batch sliced fp32 fill");
+        } else {
+            alloc(m_bsVal, sizeof(double) * ((size_t)stored + 32), "batch sliced values");
+            check(batch_sell_fill<double>(m_stream, (int)nsys, nsl, m_bSysRow.as<int>(), m_bsBase.as<int>(),
+                                          m_bRowptr.as<int>(), m_bCol.as<int>(), m_bVal.as<double>(),
+                                          m_bsOff.as<int>(), m_bsVal.as<double>(), m_bsCol.as<uint16_t>()),
+                  "batch sliced fill");
+        }
+    }
+
     BatchLaunch L;
     L.nsys = (int)nsys;
     L.sysRow = m_bSysRow.as<int>();
@@ -1488,6 +1533,13 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
         const double delta = envDouble("XJPCG_RELIABLE_DELTA", 0.01);
         L.delta2 = delta * delta;
     }
+    if (sliced) {
+        L.sliceBase = m_bsBase.as<int>();
+        L.sliceOff = m_bsOff.as<int>();
+        L.sval = mixed ? nullptr : m_bsVal.as<double>();
+        L.sval32 = mixed ? m_bsVal32.as<float>() : nullptr;
+        L.scol = m_bsCol.as<uint16_t>();
+    }
 
     // Shape candidates: CTA size x lanes per row x rows of p kept in shared
     // memory (the largest system, or a third of it for more CTAs per SM).
@@ -1495,7 +1547,8 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
     const int smemCap = (int)(200 * 1024 / esz);
     std::vector<int> smemRows = {std::min(maxN, smemCap), std::min(maxN, 4096)};
     if (smemRows[1] == smemRows[0]) smemRows.pop_back();
-    const uint64_t key = mixKey(mixKey(mixKey(nsys, (uint64_t)total), (uint64_t)nnz), (uint64_t)precision + 7);
+    const uint64_t key = mixKey(mixKey(mixKey(nsys, (uint64_t)total), (uint64_t)nnz),
+                                (uint64_t)precision + 7 + (sliced ? 1000 : 0));
     const int forced = envInt("XJPCG_BATCH_CFG", -1);
     auto runOnce = [&](int cfg, int rows, float* ms) {
         check(cudaMemsetAsync(m_bQueue.p, 0, 16, m_stream), "memset queue");
@@ -1516,6 +1569,7 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
         float best = 1e30f;
         for (size_t si = 0; si < smemRows.size(); ++si)
             for (int c = 0; c < ncfg; ++c) {
+                if (batch_config_sliced(c) && !sliced) continue;
                 float ms = 0;
                 runOnce(c, smemRows[si], &ms);
                 m_batchTuneMs[si * ncfg + c] = ms;
@@ -1673,6 +1727,7 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
         batch_config_shape(m_batchCfg, &t, &l);
         info->batchThreads = (uint32_t)t;
         info->batchLanes = (uint32_t)l;
+        info->batchSliced = batch_config_sliced(m_batchCfg) ? 1u : 0u;
     }
     info->batchSmemRows = (uint32_t)m_batchSmemRows;
     info->batchGrid = (uint32_t)m_batchGrid;

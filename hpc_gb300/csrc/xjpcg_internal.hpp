@@ -158,11 +158,24 @@ struct BatchLaunch {
     uint32_t maxIterP1;
     double tol;
     double delta2;  // mixed: reliable-update threshold, squared
+    // per-system SELL-32 copy for the sliced kernels (null: not built)
+    const int* sliceBase = nullptr;
+    const int* sliceOff = nullptr;
+    const double* sval = nullptr;
+    const float* sval32 = nullptr;
+    const uint16_t* scol = nullptr;
 };
 int batch_num_configs();
 cudaError_t batch_validate_columns(cudaStream_t st, int nsys, const int* sysRow, const int* rowptr, const int* col,
                                    int* flag);
 void batch_config_shape(int cfg, int* threads, int* lanes);
+bool batch_config_sliced(int cfg);  // the kernel reads the per-system SELL-32 copy
+cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
+                              const int* rowptr, int* sliceLen, int* sliceOff, int* blockSums);
+template <typename VT>
+cudaError_t batch_sell_fill(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
+                            const int* rowptr, const int* col, const double* val, const int* sliceOff, VT* sval,
+                            uint16_t* scol);
 cudaError_t batch_launch(int cfg, bool mixed, int numSms, int smemRows, cudaStream_t st, const BatchLaunch& L,
                          int* gridOut);
 

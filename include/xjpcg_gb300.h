@@ -44,7 +44,7 @@ typedef struct {
     uint32_t spmvCfg;      /* index of the FP64 SpMV configuration in the tuning table */
     uint32_t spmvCfg32;    /* index of the mixed solver's FP32 SpMV configuration (~0 until tuned) */
     uint32_t spmvLayout32; /* layout of that configuration, coded as spmvLayout */
-    uint32_t reserved;
+    uint32_t batchSliced;  /* batched solves: 1 when the chosen kernel reads the per-system SELL-32 copy */
     double tuneMs;         /* wall time of the last SpMV tuning (part of m_matProc) */
     double uploadMs;       /* device time of the last COO matrix upload (H2D, part of m_matProc) */
 } XJPCG_GbInfo_t;

@@ -57,6 +57,26 @@ def test_batched_maxiter_and_mask(handle, batch):
         assert abs(r["res"] - ref["res"]) <= 1e-9 * ref["res"]
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_every_kernel_shape(handle, batch, precision, monkeypatch):
+    # every kernel shape forced in turn (CSR with 1 or 2 lanes per row, and
+    # the sliced kernels over the per-system SELL-32 copy) meets the bar
+    sub = batch[:16]
+    refs = [oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10) for s in sub]
+    shapes = 0
+    for cfg in range(9):
+        monkeypatch.setenv("XJPCG_BATCH_CFG", str(cfg))
+        st, xs, res = handle.batch_solve(sub, 20000, 1e-10, precision=precision)
+        assert st == X.SUCCESS, (cfg, handle.last_message())
+        shapes += handle.info().batchSliced
+        for s, x, r, ref in zip(sub, xs, res, refs):
+            assert oracle.true_relres(s.rowptr, s.col, s.val, s.b, x) <= 1.5e-10
+            if precision == 0:
+                assert abs(int(r["iters"]) - ref["iters"]) <= max(1, int(0.01 * ref["iters"]))
+                assert np.linalg.norm(x - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
+    assert shapes == 3  # the three sliced shapes ran
+
+
 def test_batched_rejects_bad_columns(handle, batch):
     bad = [W.System(s.n, s.rowptr, s.col.copy(), s.val, s.diag, s.b) for s in batch[:2]]
     bad[1].col[3] = bad[1].n  # outside its own system
