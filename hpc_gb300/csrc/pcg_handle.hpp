@@ -198,6 +198,8 @@ class PcgHandle {
     int m_device = 0;
     int m_numSms = 0;
     cudaStream_t m_stream = nullptr;
+    cudaStream_t m_upStream = nullptr;  // COO value upload, overlapping the index conversion
+    cudaEvent_t m_evIdxIn = nullptr;
     cudaEvent_t m_ev0 = nullptr, m_ev1 = nullptr;
     uint64_t m_generation = 1;
 
