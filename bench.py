@@ -363,6 +363,32 @@ def adjoint_measure(X, nx=96):
             "tol": 1e-12, "note": "host-array calls (H2D/D2H inside); gradient checked in tests/test_gpu_adjoint.py"}
 
 
+def export_measure(X, sysm, reps=3):
+    """Device time of the signature exporter (the reference's host
+    partitioner, gen_signature.hpp:41-73, on the GPU) for the bench matrix.
+    The matrix is set again before each rep so that the layout is rebuilt."""
+    import ctypes as C
+    import torch
+    h = X.JPCG()
+    ts = []
+    sig = X.GbSignature()
+    for _ in range(reps + 1):
+        h.csr_solve(sysm.n, sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 0, 1e-10)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = h.lib.xJPCG_gbExportSignature(h.h, C.byref(sig))
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+        if st != X.SUCCESS:
+            raise RuntimeError(h.last_message())
+    out_bytes = sig.rbParamBytes + sig.parParamBytes + sum(sig.nnzValBytes[c] for c in range(16))
+    h.close()
+    return {"partition_s": float(np.median(ts[1:])), "signature_bytes": int(out_bytes),
+            "call": "xJPCG_gbExportSignature on the stored matrix (device buffers; the copy out is separate)",
+            "reference_partitioner": "SpmPar::partitionCooMat compiled from the reference sources runs on the "
+                                     "build host only (oracle/time_ref_partition.py), not here"}
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -572,6 +598,7 @@ def run_gb300(args):
                            mixed_vs_fp64(X, W.zipf_spd(2_000_000, seed=2), "zipf_spd_2M")]
         extras["batched"] = batched_measure(X)
         extras["adjoint"] = adjoint_measure(X)
+        extras["signature_export"] = export_measure(X, sysm)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,

@@ -28,6 +28,7 @@
  * Exit status 0 on success, 3 when the reference raised an exception (its
  * message goes to dir/ref_error.txt).
  */
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -36,6 +37,9 @@
 #include <sys/stat.h>
 
 #include "gen_signature.hpp"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace {
 
@@ -75,6 +79,17 @@ void dumpSorted(const std::string& dir, xf::sparse::SparseMatrix& m) {
     writeVec(dir + "/ref_sorted_data.bin", m.m_data_list);
 }
 
+// Wall time of the reference's partition call alone (no file I/O), written to
+// dir/ref_time.txt as "seconds threads" (threads = OpenMP's maximum).
+void recordTime(const std::string& dir, double s) {
+    std::ofstream t(dir + "/ref_time.txt");
+#ifdef _OPENMP
+    t << s << " " << omp_get_max_threads() << "\n";
+#else
+    t << s << " 1\n";
+#endif
+}
+
 void storeTo(const std::string& dir, xf::sparse::MatPartition& par) {
     mkdir(dir.c_str(), 0755);
     xf::sparse::storeMatPar(dir, par);
@@ -105,7 +120,9 @@ int main(int argc, char** argv) {
             xf::sparse::SparseMatrix m;
             m.loadCoo(n, n, (uint32_t)nnz, row.data(), col.data(), base);
             dumpSorted(dir, m);
+            const auto t0 = std::chrono::steady_clock::now();
             xf::sparse::MatPartition par = spm.partitionCooMat(n, n, (uint32_t)nnz, row.data(), col.data(), data.data(), base);
+            recordTime(dir, std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
             storeTo(dir + "/sig", par);
             if (exists(dir + "/data2.bin")) {
                 auto data2 = readVec<double>(dir + "/data2.bin", nnz);
@@ -121,7 +138,9 @@ int main(int argc, char** argv) {
             xf::sparse::SparseMatrix m;
             m.loadCscSym(n, full, rowIdx.data(), colPtr.data(), base);
             dumpSorted(dir, m);
+            const auto t0 = std::chrono::steady_clock::now();
             xf::sparse::MatPartition par = spm.partitionCscSymMat(n, full, rowIdx.data(), colPtr.data(), data.data(), base);
+            recordTime(dir, std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
             storeTo(dir + "/sig", par);
             if (exists(dir + "/data2.bin")) {
                 auto data2 = readVec<double>(dir + "/data2.bin", nnz);
