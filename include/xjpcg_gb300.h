@@ -77,7 +77,7 @@ XJPCG_Status_t xJPCG_gbSolveDevice(XJPCG_Handle_t* handle, const double* d_b, co
  * their search direction; a refresh folds the FP32 correction into the FP64
  * x, recomputes r = b - A x with an FP64 SpMV and restarts the FP32 residual
  * from it.  A refresh runs when the FP32 residual norm has fallen by a factor
- * delta below its largest value since the last refresh (delta = 0.01, or
+ * delta below its largest value since the last refresh (delta = 1e-3, or
  * XJPCG_RELIABLE_DELTA), when it meets the tolerance, and when the iteration
  * budget runs out.  Stops when ||b - A x|| <= tol ||b|| (true FP64 residual)
  * or after maxIter iterations.  *iter = FP32 iterations, *res = final true
