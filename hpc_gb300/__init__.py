@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbGetRecords", "xJPCG_gbGetInfo", "xJPCG_gbGetStream", "xJPCG_gbSetSpmvLanes", "xJPCG_gbSetSpmvConfig", "xJPCG_gbSetSpmvConfig32",
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
     "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv", "xJPCG_gbSetSignatureSumOrder",
-    "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32",
+    "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32", "xJPCG_gbDiagWaitTimeout",
 ]
 
 
@@ -121,6 +121,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbSetSpmvLanes.argtypes = [_P, C.c_int]
     lib.xJPCG_gbSetSpmvConfig.argtypes = [_P, C.c_int]
     lib.xJPCG_gbSetSpmvConfig32.argtypes = [_P, C.c_int]
+    lib.xJPCG_gbDiagWaitTimeout.argtypes = [_P, u64, C.POINTER(u32), C.POINTER(u64)]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbGetSpmvTuning32.argtypes = [_P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
@@ -427,6 +428,15 @@ class JPCG:
         st = self.lib.xJPCG_gbSetSpmvConfig32(self.h, cfg)
         if st != SUCCESS:
             raise XJPCGError(st, self.last_message())
+
+    def diag_wait_timeout(self, budget_ns: int):
+        """Failure-detection diagnostic (xJPCG_gbDiagWaitTimeout): a bounded
+        device wait that nothing completes.  Returns (status, device status
+        bits, wait duration in ns); status is INTERNAL_ERROR when the wait
+        gave up, as a timed-out solve reports it."""
+        dev, ns = C.c_uint32(0), C.c_uint64(0)
+        st = self.lib.xJPCG_gbDiagWaitTimeout(self.h, budget_ns, C.byref(dev), C.byref(ns))
+        return st, dev.value, ns.value
 
     def set_spmv_config(self, cfg: int):
         """Force the FP64 SpMV configuration with index cfg of spmv_tuning() (-1: tuned)."""

@@ -200,6 +200,38 @@ __global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double*
     }
 }
 
+// Diagnostic of the bounded wait that every mbarrier wait in the library
+// uses (mbar_wait_bounded).  One warp initialises an mbarrier that expects
+// one arrival and never arrives, so the wait cannot complete: it must give up
+// after budgetNs and report kStatusWaitTimeout, as a stalled copy would.  No
+// copy is issued, so nothing is in flight when the CTA exits.  out[0] =
+// status bits, out[1..2] = the wait's duration in ns.
+__global__ void wait_probe_kernel(uint64_t budgetNs, uint32_t* out) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncwarp();
+    const uint64_t t0 = globaltimer_ns();
+    const bool ok = mbar_wait_bounded(&bar, 0u, budgetNs);
+    const uint64_t dt = globaltimer_ns() - t0;
+    if (__any_sync(0xffffffffu, !ok) && threadIdx.x == 0) {
+        out[0] = kStatusWaitTimeout;
+        out[1] = (uint32_t)dt;
+        out[2] = (uint32_t)(dt >> 32);
+    } else if (threadIdx.x == 0) {
+        out[0] = 0u;
+        out[1] = (uint32_t)dt;
+        out[2] = (uint32_t)(dt >> 32);
+    }
+}
+
+cudaError_t wait_probe_launch(cudaStream_t st, uint64_t budgetNs, uint32_t* out) {
+    wait_probe_kernel<<<1, 32, 0, st>>>(budgetNs, out);
+    return cudaGetLastError();
+}
+
 // The update kernel holds two elements per step (48 registers): one wave of
 // 5 CTAs per SM.
 int update_grid(int n4, int numSms) {

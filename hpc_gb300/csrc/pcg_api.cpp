@@ -454,4 +454,13 @@ XJPCG_Status_t xJPCG_gbSetSpmvConfig32(XJPCG_Handle_t* handle, int cfg) {
     XJ_GUARD_END("FP32 SpMV configuration set successfully")
 }
 
+XJPCG_Status_t xJPCG_gbDiagWaitTimeout(XJPCG_Handle_t* handle, uint64_t budgetNs, uint32_t* deviceStatus,
+                                       uint64_t* elapsedNs) {
+    XJ_GUARD_BEGIN
+    if (deviceStatus == nullptr || elapsedNs == nullptr)
+        throw xjpcg::InvalidValue("deviceStatus and elapsedNs must not be null.");
+    p->diagWaitTimeout(budgetNs, deviceStatus, elapsedNs);
+    XJ_GUARD_END("The device wait completed")
+}
+
 }  // extern "C"

@@ -299,6 +299,23 @@ void PcgHandle::setLanes(int lanes) {
     if (m_haveMatrix) tuneSpmv();
 }
 
+// Runs the bounded-wait diagnostic on the handle's stream: a wait that can
+// never complete must give up after budgetNs and report the timeout the way a
+// solve does (INTERNAL_ERROR), and the context stays usable.
+void PcgHandle::diagWaitTimeout(uint64_t budgetNs, uint32_t* deviceStatus, uint64_t* elapsedNs) {
+    if (budgetNs == 0 || budgetNs > 1000000000ull)
+        throw InvalidValue("the wait budget must be between 1 ns and 1 s.");
+    alloc(m_diagBuf, 16, "wait diagnostic");
+    check(cudaMemsetAsync(m_diagBuf.p, 0xff, 16, m_stream), "memset");
+    check(wait_probe_launch(m_stream, budgetNs, m_diagBuf.as<uint32_t>()), "wait diagnostic");
+    uint32_t out[3] = {0u, 0u, 0u};
+    check(cudaMemcpyAsync(out, m_diagBuf.p, sizeof(out), cudaMemcpyDeviceToHost, m_stream), "wait diagnostic");
+    check(cudaStreamSynchronize(m_stream), "wait diagnostic");
+    *deviceStatus = out[0];
+    *elapsedNs = (uint64_t)out[1] | ((uint64_t)out[2] << 32);
+    if (out[0] & kStatusWaitTimeout) throw InternalError("Run kernel failed: a device wait timed out.");
+}
+
 void PcgHandle::setSpmvConfig32(int cfg) {
     if (cfg < -1) throw InvalidValue("SpMV configuration index must be -1 (tuned) or at least 0.");
     if (cfg >= numSpmvCfgs()) throw InvalidValue("no such SpMV configuration.");

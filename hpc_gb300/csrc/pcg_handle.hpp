@@ -138,6 +138,7 @@ class PcgHandle {
     void setLanes(int lanes);
     void setSpmvConfig(int cfg);
     void setSpmvConfig32(int cfg);
+    void diagWaitTimeout(uint64_t budgetNs, uint32_t* deviceStatus, uint64_t* elapsedNs);
 
     bool hasMatrix() const { return m_haveMatrix; }
     uint32_t matrixN() const { return m_n; }
@@ -241,6 +242,7 @@ class PcgHandle {
     int m_forcedCfg32 = -1;  // forced FP32 SpMV configuration of the mixed solver, -1 = tuned
     // SpMV tuning cache: the choices stand while the structure fingerprint matches
     DevBuf m_hashBuf;
+    DevBuf m_diagBuf;  // bounded-wait diagnostic output
     uint64_t m_structHash = 0, m_tunedHash = ~0ull;
     int m_tunedCfg = -1, m_tuned32Cfg = -1;
     int m_spmvCfg = 2;

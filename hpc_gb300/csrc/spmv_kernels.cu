@@ -105,11 +105,12 @@ __global__ void __launch_bounds__(NC + 32) spmv_ws_kernel(int n, int ntiles, con
     __syncthreads();
 
     AccT dacc = AccT(0);
+    int pjob = 0;  // jobs the producer issued
     if (warp == 0) {
         // ------------------------------ producer ------------------------------
         if (lane == 0) {
             const uint64_t pol = l2_policy_evict_first();
-            int job = 0;
+            int& job = pjob;
             for (int t = blockIdx.x; t < ntiles && !abortFlag; t += gridDim.x) {
                 const int r0 = t * R, r1 = min(r0 + R, n);
                 const int ts = __ldg(&rowptr[r0]), te = __ldg(&rowptr[r1]);
@@ -130,11 +131,6 @@ __global__ void __launch_bounds__(NC + 32) spmv_ws_kernel(int n, int ntiles, con
                         bulk_g2s(scol + st * Sh::CP, col + a0, cnt * 4u, &fullBar[st], pol);
                     }
                 }
-            }
-            if (abortFlag) {
-                // Drain: the last S jobs may still be in flight.
-                for (int j = max(0, job - S); j < job; ++j)
-                    mbar_wait_bounded(&fullBar[j % S], (uint32_t)(j / S) & 1u, kWaitBudgetNs);
             }
         }
         __syncwarp();
@@ -200,6 +196,10 @@ __global__ void __launch_bounds__(NC + 32) spmv_ws_kernel(int n, int ntiles, con
     __syncthreads();
     if (abortFlag) {
         if (tid == 0) {
+            // Drain: whichever side gave up, the last S jobs may still be in
+            // flight (each wait bounded; a completed one returns at once).
+            for (int j = max(0, pjob - S); j < pjob; ++j)
+                mbar_wait_bounded(&fullBar[j % S], (uint32_t)(j / S) & 1u, kWaitBudgetNs);
             atomicOr(&state->status, kStatusWaitTimeout);
             *(volatile uint32_t*)&state->done = 1u;  // later kernels of the loop stand down
         }

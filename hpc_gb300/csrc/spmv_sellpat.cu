@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(kPatThreads, 6) spmv_sellpat_kernel(
 // the other buffer.  A warp thus keeps a whole slice (3.5 KB for a 27-point
 // stencil) in flight with no registers held for it.  Slices with per-entry
 // columns, or more than kTmaCols stored columns, take the plain loads.  Every
-// wait is bounded (2 s); on expiry the warp drains its other copy (bounded),
+// wait is bounded (2 s); on expiry the warp drains both of its copies (bounded),
 // records kStatusWaitTimeout, marks the loop done and stops.  The FMAs run in
 // the plain kernel's order, so the sums are the same bit for bit.
 constexpr int kTmaCols = 32;
@@ -336,7 +336,10 @@ __global__ void __launch_bounds__(kPatThreads, 3) spmv_sellpat_tma_kernel(
                 phase0 ^= 1u;
             if (__any_sync(0xffffffffu, !ok)) {
                 abort = true;
-                if (fitsn) mbar_wait_bounded(&bars[wid][cb ^ 1], cb ? phase0 : phase1, kTmaWaitNs);  // drain
+                // drain both copies this warp may have in flight, the one it
+                // gave up on and the prefetch (each wait bounded)
+                mbar_wait_bounded(&bars[wid][cb], ph, kTmaWaitNs);
+                if (fitsn) mbar_wait_bounded(&bars[wid][cb ^ 1], cb ? phase0 : phase1, kTmaWaitNs);
                 break;
             }
             const int* p = pat + __ldg(&patOff[__ldg(&patIdx[s])]);

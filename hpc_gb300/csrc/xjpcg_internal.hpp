@@ -66,6 +66,10 @@ cudaError_t spmv_sellpat_launch(int cfg, int grid, cudaStream_t st, int n, const
                                 const int* gcol, const VT* sval, const VT* x, VT* y, const VT* b, CgState* state,
                                 double* partials, int mode, const uint32_t* doneFlag);
 
+// ---- bounded-wait diagnostic (cg_kernels.cu) ----
+// out: 3 uint32 (status bits, wait duration in ns as two halves).
+cudaError_t wait_probe_launch(cudaStream_t st, uint64_t budgetNs, uint32_t* out);
+
 // ---- length-sorted sliced SpMV (spmv_sellsort.cu) ----
 int sellsort_num_configs();
 int sellsort_config_unroll(int cfg);

@@ -248,6 +248,17 @@ XJPCG_Status_t xJPCG_gbSetSpmvConfig(XJPCG_Handle_t* handle, int cfg);
  * matrix in FP32. */
 XJPCG_Status_t xJPCG_gbSetSpmvConfig32(XJPCG_Handle_t* handle, int cfg);
 
+/* Failure-detection diagnostic.  Runs, on the handle's stream, the bounded
+ * mbarrier wait that every wait of the library uses, on a barrier that
+ * nothing completes.  The wait gives up after budgetNs (1 ns .. 1 s) and the
+ * call returns INTERNAL_ERROR with the message a timed-out solve gives;
+ * *deviceStatus = the device status bits (2 = wait timeout) and *elapsedNs =
+ * the wait's duration on the device clock.  No copy is in flight, the GPU
+ * context stays usable and the handle's matrix and vectors are untouched.
+ * INVALID_VALUE for a budget out of range or null outputs. */
+XJPCG_Status_t xJPCG_gbDiagWaitTimeout(XJPCG_Handle_t* handle, uint64_t budgetNs, uint32_t* deviceStatus,
+                                       uint64_t* elapsedNs);
+
 /* y = A x and *d_dot = x.y for callers that cannot allocate device memory.
  *
  * No counterpart in the reference.  Some callers may not allocate at the

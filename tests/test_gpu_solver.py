@@ -491,6 +491,25 @@ def test_zero_rhs_breakdown(handle):
     assert handle.info().itersRun == 1
 
 
+def test_wait_timeout_reported_and_context_usable(handle):
+    # failure detection without a fault: the library's bounded mbarrier wait
+    # on a barrier that nothing completes gives up after its budget (5 ms
+    # here, 2 s in the kernels), the host reports it as a timed-out solve
+    # does, and the same handle then solves normally
+    s = W.poisson7(16)
+    r0 = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 2000, 1e-10)
+    st, dev, ns = handle.diag_wait_timeout(5_000_000)
+    assert st == X.INTERNAL_ERROR
+    assert handle.last_message() == "INTERNAL ERROR: Run kernel failed: a device wait timed out."
+    assert dev == 2  # kStatusWaitTimeout
+    assert 5_000_000 <= ns < 1_000_000_000
+    for bad in (0, 2_000_000_000):
+        assert handle.diag_wait_timeout(bad)[0] == X.INVALID_VALUE
+    r1 = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 2000, 1e-10, mode=X.MODE_KEEP_MATRIX)
+    assert r1.status == X.SUCCESS and r1.iters == r0.iters
+    assert np.array_equal(r1.x, r0.x)
+
+
 @pytest.mark.parametrize("lanes", [0, -2])
 def test_power_law_rows_merge_path(handle, lanes):
     """Zipf rows (4 .. 4096+ entries): SpMV and a solve with the merge-path
