@@ -39,6 +39,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
     "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv", "xJPCG_gbSetSignatureSumOrder",
     "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32", "xJPCG_gbDiagWaitTimeout",
+    "xJPCG_gbDiagCheckGuards",
 ]
 
 
@@ -122,6 +123,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbSetSpmvConfig.argtypes = [_P, C.c_int]
     lib.xJPCG_gbSetSpmvConfig32.argtypes = [_P, C.c_int]
     lib.xJPCG_gbDiagWaitTimeout.argtypes = [_P, u64, C.POINTER(u32), C.POINTER(u64)]
+    lib.xJPCG_gbDiagCheckGuards.argtypes = [_P, C.POINTER(u32)]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbGetSpmvTuning32.argtypes = [_P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
@@ -437,6 +439,14 @@ class JPCG:
         dev, ns = C.c_uint32(0), C.c_uint64(0)
         st = self.lib.xJPCG_gbDiagWaitTimeout(self.h, budget_ns, C.byref(dev), C.byref(ns))
         return st, dev.value, ns.value
+
+    def check_guards(self):
+        """Memory-overrun diagnostic (xJPCG_gbDiagCheckGuards) of a handle
+        created with XJPCG_GUARD_BYTES set: (status, buffers whose guard
+        bytes changed)."""
+        bad = C.c_uint32(0)
+        st = self.lib.xJPCG_gbDiagCheckGuards(self.h, C.byref(bad))
+        return st, bad.value
 
     def set_spmv_config(self, cfg: int):
         """Force the FP64 SpMV configuration with index cfg of spmv_tuning() (-1: tuned)."""

@@ -463,4 +463,14 @@ XJPCG_Status_t xJPCG_gbDiagWaitTimeout(XJPCG_Handle_t* handle, uint64_t budgetNs
     XJ_GUARD_END("The device wait completed")
 }
 
+XJPCG_Status_t xJPCG_gbDiagCheckGuards(XJPCG_Handle_t* handle, uint32_t* corrupted) {
+    XJ_GUARD_BEGIN
+    if (corrupted == nullptr) throw xjpcg::InvalidValue("corrupted must not be null.");
+    if (!p->guardsOn()) throw xjpcg::InvalidValue("the handle was created without guard bytes (XJPCG_GUARD_BYTES).");
+    std::string first;
+    *corrupted = p->checkGuards(&first);
+    if (*corrupted) throw xjpcg::InternalError("a kernel wrote past the end of " + first);
+    XJ_GUARD_END("Guard bytes intact")
+}
+
 }  // extern "C"

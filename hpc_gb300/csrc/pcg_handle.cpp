@@ -22,18 +22,33 @@ double envDouble(const char* name, double dflt) {
     const char* v = std::getenv(name);
     return v ? std::atof(v) : dflt;
 }
+bool envIs(const char* name, const char* value) {
+    const char* v = std::getenv(name);
+    return v && std::strcmp(v, value) == 0;
+}
 }  // namespace
 
-bool DevBuf::ensure(size_t b, uint64_t* generation) {
+bool DevBuf::ensure(size_t b, uint64_t* generation, size_t guardBytes) {
     if (b == 0) b = 16;
     if (b <= bytes) return true;
     release();
-    if (cudaMalloc(&p, b) != cudaSuccess) {
+    if (cudaMalloc(&p, b + guardBytes) != cudaSuccess) {
         cudaGetLastError();
         p = nullptr;
         return false;
     }
+    if (guardBytes > 0) {
+        // Allocations happen outside stream captures; the fill completes
+        // before any kernel of the handle can touch the buffer.
+        if (cudaMemset(static_cast<unsigned char*>(p) + b, kGuardByte, guardBytes) != cudaSuccess ||
+            cudaDeviceSynchronize() != cudaSuccess) {
+            cudaGetLastError();
+            release();
+            return false;
+        }
+    }
     bytes = b;
+    guard = guardBytes;
     if (generation) ++*generation;
     return true;
 }
@@ -59,10 +74,53 @@ void PcgHandle::check(cudaError_t e, const char* what) {
 }
 
 void PcgHandle::alloc(DevBuf& b, size_t bytes, const char* what) {
-    if (!b.ensure(bytes, &m_generation)) throw AllocFailed(std::string("device allocation failed for ") + what);
+    // XJPCG_FAULT=alloc: every allocation after the handle's own set-up fails
+    // as a cudaMalloc failure would (host-side fault injection).
+    if (m_faultAlloc && m_initDone && bytes > b.bytes)
+        throw AllocFailed(std::string("device allocation failed for ") + what);
+    if (!b.ensure(bytes, &m_generation, m_guardBytes))
+        throw AllocFailed(std::string("device allocation failed for ") + what);
+    if (m_guardBytes > 0) {
+        bool known = false;
+        for (const auto& g : m_guarded) known = known || g.first == &b;
+        if (!known) m_guarded.emplace_back(&b, what);
+    }
+}
+
+// Debug handles (XJPCG_GUARD_BYTES > 0 when the handle is created) allocate
+// every buffer with guard bytes after its end, a stand-in for a memory
+// checker: a kernel that writes past the end of a buffer changes them.
+// Returns the number of buffers whose guard bytes changed.
+uint32_t PcgHandle::checkGuards(std::string* firstBad) {
+    check(cudaStreamSynchronize(m_stream), "sync");
+    check(cudaStreamSynchronize(m_upStream), "sync");
+    uint32_t bad = 0;
+    std::vector<unsigned char> host;
+    for (const auto& g : m_guarded) {
+        const DevBuf* b = g.first;
+        if (b->p == nullptr || b->guard == 0) continue;
+        host.resize(b->guard);
+        check(cudaMemcpy(host.data(), static_cast<const unsigned char*>(b->p) + b->bytes, b->guard,
+                         cudaMemcpyDeviceToHost),
+              "guard check");
+        bool ok = true;
+        for (unsigned char c : host) ok = ok && c == kGuardByte;
+        if (!ok) {
+            if (bad == 0 && firstBad) *firstBad = g.second;
+            ++bad;
+        }
+    }
+    return bad;
+}
+
+// XJPCG_FAULT=launch: the solver launches (graphs, or the first kernel of
+// the host-driven loops) report a launch failure before anything is queued.
+void PcgHandle::faultPoint(const char* what) {
+    if (m_faultLaunch) check(cudaErrorLaunchFailure, what);
 }
 
 void PcgHandle::init() {
+    m_guardBytes = (size_t)std::max(0, envInt("XJPCG_GUARD_BYTES", 0));
     check(cudaGetDevice(&m_device), "cudaGetDevice");
     check(cudaDeviceGetAttribute(&m_numSms, cudaDevAttrMultiProcessorCount, m_device), "cudaDeviceGetAttribute");
     check(cudaStreamCreateWithFlags(&m_stream, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -82,6 +140,9 @@ void PcgHandle::init() {
     m_useGraph = envInt("XJPCG_HOST_LOOP", 0) == 0;
     m_forcedLanes = envInt("XJPCG_SPMV_LANES", 0);
     m_forcedCfg = envInt("XJPCG_SPMV_CFG", -1);
+    m_faultAlloc = envIs("XJPCG_FAULT", "alloc");
+    m_faultLaunch = envIs("XJPCG_FAULT", "launch");
+    m_initDone = true;
 }
 
 // ---------------------------------------------------------------------------
@@ -902,6 +963,7 @@ Results PcgHandle::run(uint32_t maxIter, double tol) {
         cmd.useCond = 1;
         cmd.condHandle = (uint64_t)m_cond;
     }
+    faultPoint("graph launch");
     check(cudaMemcpyAsync(st, &cmd, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
     check(cudaEventRecord(m_ev0, m_stream), "event");
     if (m_useGraph) {
@@ -1068,6 +1130,7 @@ Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
     // system (22 iterations, refresh-bound) 1e-3 saves one of six refreshes.
     const double delta = envDouble("XJPCG_RELIABLE_DELTA", 1e-3);
     cmd.delta2 = delta * delta;
+    faultPoint("graph launch");
     check(cudaMemcpyAsync(st, &cmd, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
     check(cudaEventRecord(m_ev0, m_stream), "event");
     if (m_useGraph) {
@@ -1640,6 +1703,7 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
         m_batchGrid = grid;
         m_batchExecKey = gkey;
     }
+    faultPoint("graph launch");
     check(cudaEventRecord(m_ev0, m_stream), "event");
     check(cudaGraphLaunch(m_batchExec, m_stream), "graph launch");
     check(cudaEventRecord(m_ev1, m_stream), "event");

@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/pcg.h"
@@ -35,16 +36,22 @@ inline CgError ExecFailed(const std::string& s) { return CgError(XJPCG_STATUS_EX
 
 // Grow-only device buffer.  Every reallocation bumps the owner's generation
 // so graphs that captured the old address are rebuilt.
+constexpr unsigned char kGuardByte = 0xA5;
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    size_t guard = 0;  // guard bytes allocated past `bytes` (debug builds of a handle)
     ~DevBuf() { release(); }
     void release() {
         if (p) cudaFree(p);
         p = nullptr;
         bytes = 0;
+        guard = 0;
     }
-    bool ensure(size_t b, uint64_t* generation);
+    // Grows the buffer to at least b bytes; with guardBytes > 0 a new
+    // allocation carries that many bytes of kGuardByte after its end.
+    bool ensure(size_t b, uint64_t* generation, size_t guardBytes = 0);
     template <typename T>
     T* as() const {
         return static_cast<T*>(p);
@@ -139,6 +146,8 @@ class PcgHandle {
     void setSpmvConfig(int cfg);
     void setSpmvConfig32(int cfg);
     void diagWaitTimeout(uint64_t budgetNs, uint32_t* deviceStatus, uint64_t* elapsedNs);
+    uint32_t checkGuards(std::string* firstBad);  // buffers whose guard bytes changed
+    bool guardsOn() const { return m_guardBytes > 0; }
 
     bool hasMatrix() const { return m_haveMatrix; }
     uint32_t matrixN() const { return m_n; }
@@ -159,6 +168,7 @@ class PcgHandle {
 
    private:
     void check(cudaError_t e, const char* what);
+    void faultPoint(const char* what);
     void alloc(DevBuf& b, size_t bytes, const char* what);
     void finishMatrix();     // after CSR exists: values pad, tuning
     void tuneSpmv();
@@ -298,6 +308,9 @@ class PcgHandle {
     uint64_t m_mixedGen = 0;
     cudaGraphConditionalHandle m_condOuter = 0, m_condInner = 0;
     bool m_useGraph = true;
+    bool m_faultAlloc = false, m_faultLaunch = false, m_initDone = false;  // XJPCG_FAULT hooks
+    size_t m_guardBytes = 0;                                   // XJPCG_GUARD_BYTES
+    std::vector<std::pair<DevBuf*, std::string>> m_guarded;    // buffers allocated with guards
 
     // last results
     double m_lastBb = 0.0;

@@ -259,6 +259,14 @@ XJPCG_Status_t xJPCG_gbSetSpmvConfig32(XJPCG_Handle_t* handle, int cfg);
 XJPCG_Status_t xJPCG_gbDiagWaitTimeout(XJPCG_Handle_t* handle, uint64_t budgetNs, uint32_t* deviceStatus,
                                        uint64_t* elapsedNs);
 
+/* Memory-overrun diagnostic.  A handle created while the environment holds
+ * XJPCG_GUARD_BYTES=N (N > 0) allocates each of its device buffers with N
+ * bytes of 0xA5 after the end.  This call waits for the handle's streams and
+ * compares every guard: *corrupted = the number of buffers whose guard bytes
+ * changed.  SUCCESS when none did; INTERNAL_ERROR naming the first buffer
+ * when some did; INVALID_VALUE when the handle has no guards. */
+XJPCG_Status_t xJPCG_gbDiagCheckGuards(XJPCG_Handle_t* handle, uint32_t* corrupted);
+
 /* y = A x and *d_dot = x.y for callers that cannot allocate device memory.
  *
  * No counterpart in the reference.  Some callers may not allocate at the

@@ -70,6 +70,7 @@ def test_null_handle_paths(built):
     assert lib.xJPCG_gbSetSignatureSumOrder(None, 1) == X.NOT_INITIALIZED
     dev, ns = C.c_uint32(0), C.c_uint64(0)
     assert lib.xJPCG_gbDiagWaitTimeout(None, 1000, C.byref(dev), C.byref(ns)) == X.NOT_INITIALIZED
+    assert lib.xJPCG_gbDiagCheckGuards(None, C.byref(dev)) == X.NOT_INITIALIZED
 
 
 def test_struct_layouts():

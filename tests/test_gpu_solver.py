@@ -510,6 +510,47 @@ def test_wait_timeout_reported_and_context_usable(handle):
     assert np.array_equal(r1.x, r0.x)
 
 
+@pytest.mark.parametrize("fault", ["alloc", "launch"])
+def test_host_fault_injection(monkeypatch, fault):
+    # XJPCG_FAULT, read when a handle is created, injects on the host the
+    # failures the C ABI maps to ALLOC_FAILED (a device allocation fails) and
+    # INTERNAL_ERROR (a solver launch fails before anything is queued); no GPU
+    # work faults.  A handle created without it then solves normally.
+    s = W.poisson7(8)
+    rows, cols, vals = s.coo()
+    monkeypatch.setenv("XJPCG_FAULT", fault)
+    h = X.JPCG()
+    try:
+        r = h.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 100, 1e-10)
+        if fault == "alloc":
+            assert r.status == X.ALLOC_FAILED
+            assert "device allocation failed for" in h.last_message()
+        else:
+            assert r.status == X.INTERNAL_ERROR
+            assert "graph launch" in h.last_message() and "launch failure" in h.last_message()
+            assert h.mixed_solve(s.b, s.diag, 100, 1e-10).status == X.INTERNAL_ERROR
+            assert h.batch_solve([s, s], 100, 1e-10)[0] == X.INTERNAL_ERROR
+    finally:
+        h.close()
+    monkeypatch.delenv("XJPCG_FAULT")
+    h = X.JPCG()
+    try:
+        _check_solve(s, h.coo_solve(s.n, rows, cols, vals, s.diag, s.b, 2000, 1e-10))
+    finally:
+        h.close()
+
+
+def test_nan_rhs_stops_with_execution_failed(handle):
+    # a NaN in b makes alpha NaN at the first iteration: the loop stops there
+    # with EXECUTION_FAILED instead of running to maxIter
+    s = W.poisson7(8)
+    b = s.b.copy()
+    b[5] = np.nan
+    r = handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, b, 50, 1e-10)
+    assert r.status == X.EXECUTION_FAILED
+    assert handle.info().itersRun == 1
+
+
 @pytest.mark.parametrize("lanes", [0, -2])
 def test_power_law_rows_merge_path(handle, lanes):
     """Zipf rows (4 .. 4096+ entries): SpMV and a solve with the merge-path
