@@ -1,6 +1,8 @@
 // pcg_handle.cpp -- host orchestration of the GB300 xJPCG solver.
 #include "pcg_handle.hpp"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -10,6 +12,15 @@
 namespace xjpcg {
 
 namespace {
+// NVTX range over a host phase (header-only NVTX v3; a no-op unless a
+// profiler is attached), so a timeline shows matrix set-up, tuning and
+// solves by name.
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 constexpr uint64_t kMaxRecords = 1ull << 20;  // ring of records beyond this
 constexpr int kPartialSlots = 4 * 8192;       // doubles; >= 2 * max grid
 constexpr int kMaxOuter = 64;
@@ -150,6 +161,7 @@ void PcgHandle::init() {
 // ---------------------------------------------------------------------------
 void PcgHandle::setCooMat(uint32_t n, uint64_t nnz, const uint32_t* row, const uint32_t* col, const double* data,
                           int base) {
+    Range range_("xJPCG matrix set-up (COO)");
     if (nnz > 0x7ffffff0ull) throw InvalidValue("number of non-zeros exceeds 2^31 - 16.");
     m_haveMatrix = false;
     alloc(m_inRow, sizeof(uint32_t) * nnz, "COO rows");
@@ -202,6 +214,7 @@ void PcgHandle::setCooMat(uint32_t n, uint64_t nnz, const uint32_t* row, const u
 }
 
 void PcgHandle::updateCooValues(uint32_t n, uint64_t nnz, const double* data) {
+    Range range_("xJPCG values update");
     // Signature::checkUpdateDim (signature.hpp:575-583) raises SpmInvalidValue,
     // which the reference reports as INTERNAL_ERROR through std::exception.
     if (!m_haveMatrix || n != m_n || nnz != m_nnz)
@@ -217,6 +230,7 @@ void PcgHandle::updateCooValues(uint32_t n, uint64_t nnz, const double* data) {
 
 void PcgHandle::setCsrMat(uint32_t n, uint64_t nnz, const int32_t* rowPtr, const int32_t* colIdx,
                           const double* data, int base) {
+    Range range_("xJPCG matrix set-up (CSR)");
     // Row indices are expanded on the host side of the copy: the CSR row
     // pointer is small (n + 1) and validated here; the rest is the COO path.
     if ((int64_t)rowPtr[0] - base != 0 || (uint64_t)((int64_t)rowPtr[n] - base) != nnz)
@@ -235,6 +249,7 @@ void PcgHandle::updateCsrValues(uint32_t n, uint64_t nnz, const double* data) { 
 
 void PcgHandle::setCscSymMat(uint32_t n, uint64_t nnzHalf, const int64_t* rowIdx, const int64_t* colPtr,
                              const double* data, int base) {
+    Range range_("xJPCG matrix set-up (CSC)");
     // PCGImpl::setCscSymMat: full nnz = 2 * nnz - n (pcgImp.hpp:87).
     const uint64_t nnzFull = (uint32_t)(nnzHalf * 2 - n);
     if (base == 1 && colPtr[0] < 1)
@@ -735,6 +750,7 @@ int PcgHandle::timeConfigs(bool fp32, std::vector<float>& out) {
 }
 
 void PcgHandle::tuneSpmv() {
+    Range range_("xJPCG SpMV tuning");
     const auto t0 = std::chrono::steady_clock::now();
     struct TuneClock {
         std::chrono::steady_clock::time_point t0;
@@ -827,6 +843,7 @@ void PcgHandle::ensureValues32(int cfg) {
 // forced layout (XJPCG_SPMV_LANES / _CFG or xJPCG_gbSetSpmvLanes) the FP64
 // choice is kept.
 void PcgHandle::tuneSpmv32() {
+    Range range_("xJPCG FP32 SpMV tuning");
     if (m_tuned32Gen == m_structGen && m_spmvCfg32 >= 0) return;
     const int ncfg = numSpmvCfgs();
     const size_t vb32 = sizeof(float) * ((size_t)m_n4 + 4);
@@ -941,6 +958,7 @@ void PcgHandle::buildGraph() {
 }
 
 Results PcgHandle::run(uint32_t maxIter, double tol) {
+    Range range_("xJPCG fp64 solve");
     if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
     // Records: slot 0 + one per iteration, up to a ring of kMaxRecords.
     const uint64_t want = std::min<uint64_t>((uint64_t)maxIter + 2, kMaxRecords);
@@ -1107,6 +1125,7 @@ void PcgHandle::buildMixedGraph() {
 }
 
 Results PcgHandle::runMixed(uint32_t maxIter, double tol) {
+    Range range_("xJPCG mixed solve");
     if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
     const size_t vb32 = sizeof(float) * ((size_t)m_n4 + 4);
     alloc(m_r32, vb32, "r32");
@@ -1239,6 +1258,7 @@ uint16_t rdU16(const unsigned char* p, uint64_t off) {
 // dummy.  Chunks follow gen_nnzStore (signature.hpp:361-426).
 void PcgHandle::setSignatureMatrix(uint32_t nch, const void* const* bufs, const uint64_t* bytes, const void* par,
                                    uint64_t parBytes, const void* rb, uint64_t rbBytes) {
+    Range range_("xJPCG signature matrix set-up");
     if (nch != 16) throw InvalidValue("the partitioned format has 16 channels.");
     const unsigned char* R = static_cast<const unsigned char*>(rb);
     const unsigned char* P = static_cast<const unsigned char*>(par);
@@ -1429,6 +1449,7 @@ void PcgHandle::signatureSpmv(const double* x, uint32_t xLen, double* y, uint32_
 // ---------------------------------------------------------------------------
 Results PcgHandle::adjoint(const double* g, const double* diag, double* lambda, double* gradA, uint32_t maxIter,
                            double tol, bool onDevice) {
+    Range range_("xJPCG adjoint solve");
     if (!m_haveMatrix || !m_haveX) throw InvalidValue("the adjoint needs a completed solve on this handle.");
     const size_t vb = sizeof(double) * ((size_t)m_n4 + 4);
     alloc(m_xKeep, vb, "adjoint x");
@@ -1457,6 +1478,7 @@ Results PcgHandle::adjoint(const double* g, const double* diag, double* lambda, 
 
 void PcgHandle::edgeGrad(int64_t m, const int32_t* ei, const int32_t* ej, const double* c, double* grad,
                          bool onDevice) {
+    Range range_("xJPCG edge gradient");
     if (!m_haveLambda) throw InvalidValue("the edge gradient needs a completed adjoint solve.");
     if (m <= 0) throw InvalidValue("number of edges must be positive.");
     const int* dI = ei;
@@ -1495,6 +1517,7 @@ __attribute__((unused)) uint64_t mixKey(uint64_t h, uint64_t v) { return (h ^ v)
 uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32_t* rowPtr, const int32_t* colIdx,
                                const double* values, const double* diag, const double* b, double* x,
                                uint32_t maxIter, double tol, int precision, BatchResult* results, bool onDevice) {
+    Range range_("xJPCG batched solve");
     if (nsys == 0) throw InvalidValue("number of systems is zero.");
     if (precision != 0 && precision != 1) throw InvalidValue("precision must be 0 (fp64) or 1 (mixed).");
     const bool mixed = precision == 1;
@@ -1738,6 +1761,7 @@ void PcgHandle::getCsr(int32_t* rowPtr, int32_t* colIdx, double* values, uint32_
 }
 
 void PcgHandle::exportSignature(XJPCG_GbSignature_t* sig) {
+    Range range_("xJPCG signature export");
     if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");
     if (!m_sigExport.valid || m_sigExport.structGen != m_structGen) {
         m_sigExport.build(m_stream, m_n, m_nnz, m_rowptr.as<int>(), m_col.as<int>());
