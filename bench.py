@@ -300,6 +300,12 @@ def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
                                          on_device=True))
     inf = h.info()
     xm = d_x.cpu().numpy()
+    # FP32 SpMV on the HBM roofline: 4 B values + the layout's column bytes
+    # per entry, row pointers, x read once and y written once in FP32
+    ms32 = h.spmv_tuning32()[inf.spmvCfg32] if inf.spmvCfg32 < 64 else -1.0
+    b32 = (4 + LAYOUTS[inf.spmvLayout32][2]) * sysm.nnz + 4 * (sysm.n + 1) + 8 * sysm.n
+    peak, _ = measured_peak()
+    gbs32 = b32 / (ms32 / 1e3) / 1e9 if ms32 > 0 else None
     tight = oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 200000, tight_tol)["x"]
     nt = np.linalg.norm(tight)
     out = {"system": name, "n": sysm.n, "nnz": sysm.nnz, "fp64_time_to_tol_s": t64, "fp64_iters": it64,
@@ -313,7 +319,10 @@ def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
            "spmv_fp32_ms": (h.spmv_tuning32()[inf.spmvCfg32] if inf.spmvCfg32 < 64 else None),
            "spmv_fp64_ms": h.spmv_tuning()[inf.spmvCfg][4],
            "spmv_fp32_shape": (list(h.spmv_tuning()[inf.spmvCfg32][:4]) if inf.spmvCfg32 < 64 else None),
-           "spmv_tuning_fp32_ms": [round(v, 4) for v in h.spmv_tuning32()]}
+           "spmv_tuning_fp32_ms": [round(v, 4) for v in h.spmv_tuning32()],
+           "spmv_fp32_roofline": {"bytes_per_launch": b32, "achieved_gbs": gbs32,
+                                  "frac": (gbs32 / peak if gbs32 else None), "peak_gbs": peak,
+                                  "note": "tuner's median time of the chosen FP32 configuration"}}
     h.close()
     return out
 
