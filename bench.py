@@ -13,6 +13,13 @@ the path has no data exchange).
          the tuner's choice (timed on the first call, reused while the
          structure fingerprint matches), the solve and the D2H copy of x
          inside the timed region; W untimed calls first, as for value.
+  roofline  the tuner's SpMV timed alone (20 launches) against the measured
+         HBM copy bandwidth, with its FP64-issue fraction; other_layouts
+         times the int16-offset and int32-column sliced layouts the same way.
+  extras (rank 0; --no-extras skips them): mixed vs fp64 on 160^3 and on
+         the Zipf 2M system, with the FP32 SpMV's roofline; the 4,096-system
+         batch in both precisions; the 96^3 adjoint; the device time of the
+         signature exporter on the bench matrix.
 
 ``--impl reference`` times the oracle (the C/OpenMP restatement of the
 reference's JPCG; the reference itself only runs on an Alveo U280) on the
