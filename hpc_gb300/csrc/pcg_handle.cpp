@@ -23,7 +23,6 @@ struct Range {
 };
 constexpr uint64_t kMaxRecords = 1ull << 20;  // ring of records beyond this
 constexpr int kPartialSlots = 4 * 8192;       // doubles; >= 2 * max grid
-constexpr int kMaxOuter = 64;
 
 int envInt(const char* name, int dflt) {
     const char* v = std::getenv(name);
