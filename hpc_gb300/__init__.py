@@ -39,7 +39,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
     "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv", "xJPCG_gbSetSignatureSumOrder",
     "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32", "xJPCG_gbDiagWaitTimeout",
-    "xJPCG_gbDiagCheckGuards",
+    "xJPCG_gbDiagCheckGuards", "xJPCG_gbDiagFp64Rate",
 ]
 
 
@@ -124,6 +124,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbSetSpmvConfig32.argtypes = [_P, C.c_int]
     lib.xJPCG_gbDiagWaitTimeout.argtypes = [_P, u64, C.POINTER(u32), C.POINTER(u64)]
     lib.xJPCG_gbDiagCheckGuards.argtypes = [_P, C.POINTER(u32)]
+    lib.xJPCG_gbDiagFp64Rate.argtypes = [_P, C.c_int32, C.POINTER(dbl), C.POINTER(dbl)]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbGetSpmvTuning32.argtypes = [_P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
@@ -439,6 +440,15 @@ class JPCG:
         dev, ns = C.c_uint32(0), C.c_uint64(0)
         st = self.lib.xJPCG_gbDiagWaitTimeout(self.h, budget_ns, C.byref(dev), C.byref(ns))
         return st, dev.value, ns.value
+
+    def fp64_rate(self, iters: int = 16384):
+        """FP64 issue-rate diagnostic (xJPCG_gbDiagFp64Rate): (DFMA per second
+        over the whole GPU, best launch time in ms)."""
+        rate, ms = C.c_double(0.0), C.c_double(0.0)
+        st = self.lib.xJPCG_gbDiagFp64Rate(self.h, iters, C.byref(rate), C.byref(ms))
+        if st != SUCCESS:
+            raise XJPCGError(st, self.last_message())
+        return rate.value, ms.value
 
     def check_guards(self):
         """Memory-overrun diagnostic (xJPCG_gbDiagCheckGuards) of a handle

@@ -53,14 +53,14 @@ __global__ void edge_check_kernel(int64_t m, int n, const int* __restrict__ ei, 
 
 cudaError_t grad_nnz_launch(cudaStream_t st, int n, const int* rowptr, const int* col, const uint32_t* perm,
                             const double* x, const double* lambda, double* grad) {
-    const int grid = std::max(1, std::min((int)(((int64_t)n * 32 + 255) / 256), 152 * 32));
+    const int grid = std::max(1, std::min((int)(((int64_t)n * 32 + 255) / 256), device_sm_count() * 32));
     grad_nnz_kernel<<<grid, 256, 0, st>>>(n, rowptr, col, perm, x, lambda, grad);
     return cudaGetLastError();
 }
 
 cudaError_t edge_grad_launch(cudaStream_t st, int64_t m, int n, const int* ei, const int* ej, const double* c,
                              const double* x, const double* lambda, double* grad, int* flag, int* hostBad) {
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 152 * 32));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, device_sm_count() * 32));
     cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
     edge_check_kernel<<<grid, 256, 0, st>>>(m, n, ei, ej, flag);

@@ -519,7 +519,7 @@ cudaError_t batch_validate_columns(cudaStream_t st, int nsys, const int* sysRow,
                                    int* flag) {
     cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const int grid = std::max(1, std::min((nsys * 32 + 255) / 256, 152 * 16));
+    const int grid = std::max(1, std::min((nsys * 32 + 255) / 256, device_sm_count() * 16));
     batch_validate_kernel<<<grid, 256, 0, st>>>(nsys, sysRow, rowptr, col, flag);
     return cudaGetLastError();
 }
@@ -594,7 +594,7 @@ __global__ void bsell_fill_kernel(int nsys, int nslices, const int* __restrict__
 
 cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
                               const int* rowptr, int* sliceLen, int* sliceOff, int* blockSums) {
-    const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, 152 * 32));
+    const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, device_sm_count() * 32));
     bsell_width_kernel<<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, sliceLen);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -605,7 +605,7 @@ template <typename VT>
 cudaError_t batch_sell_fill(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
                             const int* rowptr, const int* col, const double* val, const int* sliceOff, VT* sval,
                             uint16_t* scol) {
-    const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, 152 * 32));
+    const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, device_sm_count() * 32));
     bsell_fill_kernel<VT><<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, col, val, sliceOff, sval,
                                                 scol);
     return cudaGetLastError();

@@ -232,6 +232,38 @@ cudaError_t wait_probe_launch(cudaStream_t st, uint64_t budgetNs, uint32_t* out)
     return cudaGetLastError();
 }
 
+// FP64 issue-rate probe: the ceiling every fp64 kernel of the loop is held
+// against.  Each thread runs kFp64Chains independent register-resident chains
+// a <- fma(a, m, c) for `iters` steps (enough independent chains per warp to
+// cover the pipe's latency at full occupancy), so the kernel issues nothing
+// but DFMA once its few loads are done.  m < 1 keeps the chains finite; one
+// store of their sum per thread keeps the compiler from removing them.
+constexpr int kFp64Chains = 8;
+
+__global__ void __launch_bounds__(kVecThreads) fp64_rate_kernel(int iters, double m, double c, double* out) {
+    double a[kFp64Chains];
+#pragma unroll
+    for (int j = 0; j < kFp64Chains; ++j) a[j] = (double)(threadIdx.x + j) * 1e-3;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < kFp64Chains; ++j) a[j] = fma(a[j], m, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < kFp64Chains; ++j) s += a[j];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// Full occupancy: 2048 threads per SM.
+int fp64_rate_grid(int numSms) { return numSms * (2048 / kVecThreads); }
+
+double fp64_rate_dfma(int grid, int iters) { return (double)grid * kVecThreads * kFp64Chains * (double)iters; }
+
+cudaError_t fp64_rate_launch(cudaStream_t st, int grid, int iters, double* out) {
+    fp64_rate_kernel<<<grid, kVecThreads, 0, st>>>(iters, 0.999999, 1e-6, out);
+    return cudaGetLastError();
+}
+
 // The update kernel holds two elements per step (48 registers): one wave of
 // 5 CTAs per SM.
 int update_grid(int n4, int numSms) {

@@ -279,7 +279,7 @@ __global__ void f64_to_f32_kernel(int64_t count, const double* __restrict__ src,
 static int grid_for(int64_t work, int threads) {
     int64_t g = (work + threads - 1) / threads;
     if (g < 1) g = 1;
-    if (g > 152 * 32) g = 152 * 32;
+    if (g > device_sm_count() * 32) g = device_sm_count() * 32;
     return (int)g;
 }
 

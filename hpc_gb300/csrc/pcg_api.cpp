@@ -463,6 +463,13 @@ XJPCG_Status_t xJPCG_gbDiagWaitTimeout(XJPCG_Handle_t* handle, uint64_t budgetNs
     XJ_GUARD_END("The device wait completed")
 }
 
+XJPCG_Status_t xJPCG_gbDiagFp64Rate(XJPCG_Handle_t* handle, int32_t iters, double* dfmaPerSecond, double* ms) {
+    XJ_GUARD_BEGIN
+    if (dfmaPerSecond == nullptr || ms == nullptr) throw xjpcg::InvalidValue("dfmaPerSecond and ms must not be null.");
+    p->diagFp64Rate(iters, dfmaPerSecond, ms);
+    XJ_GUARD_END("FP64 rate measured")
+}
+
 XJPCG_Status_t xJPCG_gbDiagCheckGuards(XJPCG_Handle_t* handle, uint32_t* corrupted) {
     XJ_GUARD_BEGIN
     if (corrupted == nullptr) throw xjpcg::InvalidValue("corrupted must not be null.");

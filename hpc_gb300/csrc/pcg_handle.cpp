@@ -391,6 +391,36 @@ void PcgHandle::diagWaitTimeout(uint64_t budgetNs, uint32_t* deviceStatus, uint6
     if (out[0] & kStatusWaitTimeout) throw InternalError("Run kernel failed: a device wait timed out.");
 }
 
+// Times the FP64 issue-rate probe on the handle's stream with CUDA events:
+// one warm-up launch, then the best of three timed launches.
+void PcgHandle::diagFp64Rate(int32_t iters, double* dfmaPerSecond, double* ms) {
+    if (iters < 1 || iters > (1 << 24)) throw InvalidValue("iters must be between 1 and 2^24.");
+    const int grid = fp64_rate_grid(m_numSms);
+    alloc(m_diagBuf, (size_t)grid * 256 * sizeof(double), "fp64 rate diagnostic");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    check(cudaEventCreate(&e0), "cudaEventCreate");
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        throw InternalError("cudaEventCreate failed.");
+    }
+    float best = -1.0f;
+    cudaError_t err = fp64_rate_launch(m_stream, grid, iters, m_diagBuf.as<double>());
+    for (int rep = 0; rep < 3 && err == cudaSuccess; ++rep) {
+        err = cudaEventRecord(e0, m_stream);
+        if (err == cudaSuccess) err = fp64_rate_launch(m_stream, grid, iters, m_diagBuf.as<double>());
+        if (err == cudaSuccess) err = cudaEventRecord(e1, m_stream);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float t = 0.0f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+        if (err == cudaSuccess && (best < 0.0f || t < best)) best = t;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check(err, "fp64 rate diagnostic");
+    *ms = best;
+    *dfmaPerSecond = best > 0.0f ? fp64_rate_dfma(grid, iters) / (best * 1e-3) : 0.0;
+}
+
 void PcgHandle::setSpmvConfig32(int cfg) {
     if (cfg < -1) throw InvalidValue("SpMV configuration index must be -1 (tuned) or at least 0.");
     if (cfg >= numSpmvCfgs()) throw InvalidValue("no such SpMV configuration.");

@@ -146,6 +146,7 @@ class PcgHandle {
     void setSpmvConfig(int cfg);
     void setSpmvConfig32(int cfg);
     void diagWaitTimeout(uint64_t budgetNs, uint32_t* deviceStatus, uint64_t* elapsedNs);
+    void diagFp64Rate(int32_t iters, double* dfmaPerSecond, double* ms);
     uint32_t checkGuards(std::string* firstBad);  // buffers whose guard bytes changed
     bool guardsOn() const { return m_guardBytes > 0; }
 

@@ -76,7 +76,7 @@ __device__ __forceinline__ int upper_index(const int* a, int cnt, int v) {
 }
 
 int grid_of(int64_t work, int threads) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>((work + threads - 1) / threads, 152 * 32));
+    return (int)std::max<int64_t>(1, std::min<int64_t>((work + threads - 1) / threads, device_sm_count() * 32));
 }
 }  // namespace
 

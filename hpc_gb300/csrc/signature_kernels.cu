@@ -129,14 +129,14 @@ __global__ void sig_ordered_spmv_kernel(int rows, const int* __restrict__ runPtr
 }
 
 cudaError_t sig_run_rows(cudaStream_t st, int64_t runs, const uint32_t* row, uint32_t* runRow, uint32_t* runIdx) {
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((runs + 255) / 256, 152 * 16));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((runs + 255) / 256, device_sm_count() * 16));
     sig_run_rows_kernel<<<grid, 256, 0, st>>>(runs, row, runRow, runIdx);
     return cudaGetLastError();
 }
 
 cudaError_t sig_ordered_spmv(cudaStream_t st, int rows, const int* runPtr, const int* runIdx, const double* val,
                              const uint32_t* col, const double* x, double* y) {
-    const int grid = std::max(1, std::min((rows + 127) / 128, 152 * 16));
+    const int grid = std::max(1, std::min((rows + 127) / 128, device_sm_count() * 16));
     sig_ordered_spmv_kernel<<<grid, 128, 0, st>>>(rows, runPtr, runIdx, val, col, x, y);
     return cudaGetLastError();
 }
@@ -144,7 +144,7 @@ cudaError_t sig_ordered_spmv(cudaStream_t st, int rows, const int* runPtr, const
 cudaError_t sig_decode(cudaStream_t st, int nchunks, const SigChunk* chunks, const unsigned char* buf, int64_t groups,
                        uint32_t* row, uint32_t* col, double* val, int* keep) {
     if (groups <= 0) return cudaSuccess;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((groups + 255) / 256, 152 * 32));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((groups + 255) / 256, device_sm_count() * 32));
     sig_decode_kernel<<<grid, 256, 0, st>>>(nchunks, chunks, buf, groups, row, col, val, keep);
     return cudaGetLastError();
 }
@@ -152,7 +152,7 @@ cudaError_t sig_decode(cudaStream_t st, int nchunks, const SigChunk* chunks, con
 cudaError_t sig_compact(cudaStream_t st, int64_t count, const int* pos, const int* keep, const uint32_t* row,
                         const uint32_t* col, const double* val, uint32_t* rowOut, uint32_t* colOut, double* valOut) {
     if (count <= 0) return cudaSuccess;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, 152 * 32));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, device_sm_count() * 32));
     sig_compact_kernel<<<grid, 256, 0, st>>>(count, pos, keep, row, col, val, rowOut, colOut, valOut);
     return cudaGetLastError();
 }
@@ -182,7 +182,7 @@ __global__ void transy_frame_kernel(uint32_t startAddr, uint32_t rows, const dou
 
 cudaError_t transy_frame(cudaStream_t st, uint32_t startAddr, uint32_t rows, const double* y, unsigned char* frame) {
     const uint32_t total = 16 + (rows == 0 ? 1u : (rows + 7) / 8) * 16;
-    const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((total + 255) / 256, 152 * 16));
+    const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((total + 255) / 256, device_sm_count() * 16));
     transy_frame_kernel<<<grid, 256, 0, st>>>(startAddr, rows, y, frame);
     return cudaGetLastError();
 }

@@ -539,7 +539,7 @@ bool sell_config_narrow(int cfg) { return cfg >= 3; }
 cudaError_t sell_build(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val, int* sliceOff,
                        int* blockSums, int64_t* total) {
     const int nslices = (n + 31) / 32;
-    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, 152 * 64);
+    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, device_sm_count() * 64);
     sell_slice_len_kernel<<<grid, 256, 0, st>>>(n, rowptr, sliceOff);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -558,7 +558,7 @@ cudaError_t sell_build(cudaStream_t st, int n, const int* rowptr, const int* col
 cudaError_t sell_narrow_fits(cudaStream_t st, int n, const int* rowptr, const int* col, int* flag, bool* fits) {
     cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n + 255) / 256, 152 * 16));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n + 255) / 256, device_sm_count() * 16));
     sell_width_kernel<<<grid, 256, 0, st>>>(n, rowptr, col, flag);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -573,7 +573,7 @@ cudaError_t sell_narrow_fits(cudaStream_t st, int n, const int* rowptr, const in
 cudaError_t sell_fill_narrow(cudaStream_t st, int n, const int* rowptr, const int* col, const int* sliceOff,
                              int16_t* scol16) {
     const int nslices = (n + 31) / 32;
-    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, 152 * 64);
+    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, device_sm_count() * 64);
     sell_fill_narrow_kernel<<<grid, 256, 0, st>>>(n, rowptr, col, sliceOff, scol16);
     return cudaGetLastError();
 }
@@ -582,7 +582,7 @@ template <typename VT>
 cudaError_t sell_fill(cudaStream_t st, int n, const int* rowptr, const int* col, const double* val,
                       const int* sliceOff, int* scol, VT* sval) {
     const int nslices = (n + 31) / 32;
-    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, 152 * 64);
+    int grid = (int)std::min<int64_t>(((int64_t)nslices * 32 + 255) / 256, device_sm_count() * 64);
     sell_fill_kernel<VT><<<grid, 256, 0, st>>>(n, rowptr, col, val, sliceOff, scol, sval);
     return cudaGetLastError();
 }

@@ -267,14 +267,14 @@ __global__ void merge_partition_kernel(int n, int nnz, int ntiles, const int* __
 
 cudaError_t merge_partition(cudaStream_t st, int n, int nnz, const int* rowptr, int* tileRow) {
     const int ntiles = (int)(((int64_t)n + nnz + kTile - 1) / kTile);
-    const int grid = std::max(1, std::min((ntiles + 256) / 256, 152 * 8));
+    const int grid = std::max(1, std::min((ntiles + 256) / 256, device_sm_count() * 8));
     merge_partition_kernel<<<grid, 256, 0, st>>>(n, nnz, ntiles, rowptr, tileRow);
     return cudaGetLastError();
 }
 
 int merge_tiles(int n, int64_t nnz) { return (int)((n + nnz + kTile - 1) / kTile); }
 int merge_items_per_thread() { return kItems; }
-int merge_fixup_grid(int ntiles) { return std::max(1, std::min((ntiles + kMT - 1) / kMT, 152 * 4)); }
+int merge_fixup_grid(int ntiles) { return std::max(1, std::min((ntiles + kMT - 1) / kMT, device_sm_count() * 4)); }
 
 template <typename VT>
 cudaError_t spmv_merge_launch(cudaStream_t st, int n, int nnz, const int* rowptr, const int* col, const VT* val,
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(kMT) residual_finish_kernel(int n, const VT* _
 template <typename VT>
 cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, double* partials, CgState* state,
                                    const uint32_t* doneFlag) {
-    const int grid = std::max(1, std::min((n + kMT - 1) / kMT, 152 * 8));
+    const int grid = std::max(1, std::min((n + kMT - 1) / kMT, device_sm_count() * 8));
     residual_finish_kernel<VT><<<grid, kMT, 0, st>>>(n, b, y, partials, state, doneFlag);
     return cudaGetLastError();
 }

@@ -27,10 +27,13 @@
 //   - every call shares the array; calls whose kernels overlap on the GPU
 //     (different streams, no ordering) race on it.  Calls on one stream are
 //     ordered and safe.
-//   - the first call on a device looks the array's device address up with
-//     cudaGetSymbolAddress (with that device current) and caches it; make that
-//     first call before any stream capture.  No call allocates, frees or calls
-//     an allocating library routine.
+//   - the first call in a CUDA context (normally: the first call on a device,
+//     in its primary context) looks the array's device address up with
+//     cudaGetSymbolAddress, with that context current, and caches it for that
+//     context; make that first call before any stream capture.  A context
+//     created later (cudaDeviceReset, cuCtxCreate) gets its own lookup.  No
+//     call allocates, frees or calls an allocating library routine.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -47,7 +50,6 @@ constexpr int kLanes = 8;                      // lanes per row
 constexpr int kRows = kThreads / kLanes;       // rows per CTA
 constexpr int kMaxTiles = 16384;               // partial sums the scratch holds
 constexpr uint32_t kMaxRows = (uint32_t)kMaxTiles * kRows;
-constexpr int kMaxDevices = 64;
 
 struct alignas(256) NoAllocScratch {
     uint32_t ticket;          // last-CTA counter; cleared before every launch
@@ -86,8 +88,64 @@ __global__ void __launch_bounds__(kThreads) spmv_dot_noalloc_kernel(uint32_t n, 
     if (grid_sum_last<kThreads, 1>(v, scr->partials, &scr->ticket, fin) && threadIdx.x == 0) *dot = fin[0];
 }
 
+// The array's device address depends on the CUDA context the library's
+// module is loaded in: the device's primary context, a context the caller
+// created with cuCtxCreate, or a primary context re-created after
+// cudaDeviceReset.  The address is therefore cached per context, keyed by the
+// driver's unique context id (cuCtxGetId), and looked up with
+// cudaGetSymbolAddress once for each new context, with that context current.
+// The driver functions are reached through cudaGetDriverEntryPointByVersion,
+// so the library does not link libcuda itself.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+struct ScratchSlot {
+    unsigned long long ctxId;
+    NoAllocScratch* addr;
+};
+constexpr int kSlots = 64;
+
 std::mutex g_setupMutex;
-NoAllocScratch* g_scratchAddr[kMaxDevices] = {};
+ScratchSlot g_slots[kSlots] = {};
+int g_slotsUsed = 0, g_slotNext = 0;
+CtxGetCurrentFn g_ctxGetCurrent = nullptr;
+CtxGetIdFn g_ctxGetId = nullptr;
+
+// Address of the scratch array in the current context (nullptr on failure).
+// Called with g_setupMutex held.
+NoAllocScratch* scratch_for_current_context() {
+    if (g_ctxGetCurrent == nullptr || g_ctxGetId == nullptr) {
+        void* f0 = nullptr;
+        void* f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0, q1;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || f0 == nullptr || f1 == nullptr)
+            return nullptr;
+        g_ctxGetCurrent = reinterpret_cast<CtxGetCurrentFn>(f0);
+        g_ctxGetId = reinterpret_cast<CtxGetIdFn>(f1);
+    }
+    CUcontext ctx = nullptr;
+    void* first = nullptr;
+    if (g_ctxGetCurrent(&ctx) != CUDA_SUCCESS) return nullptr;
+    if (ctx == nullptr) {
+        // No context is current on this thread yet: the lookup itself makes
+        // the current device's primary context current.
+        if (cudaGetSymbolAddress(&first, g_noallocScratch) != cudaSuccess || first == nullptr) return nullptr;
+        if (g_ctxGetCurrent(&ctx) != CUDA_SUCCESS || ctx == nullptr) return nullptr;
+    }
+    unsigned long long id = 0;
+    if (g_ctxGetId(ctx, &id) != CUDA_SUCCESS) return nullptr;
+    for (int i = 0; i < g_slotsUsed; ++i)
+        if (g_slots[i].ctxId == id) return g_slots[i].addr;
+    void* p = first;
+    if (p == nullptr && (cudaGetSymbolAddress(&p, g_noallocScratch) != cudaSuccess || p == nullptr)) return nullptr;
+    // A new context: take a free slot, else replace the oldest entry.
+    const int slot = g_slotsUsed < kSlots ? g_slotsUsed++ : (g_slotNext++ % kSlots);
+    g_slots[slot].ctxId = id;
+    g_slots[slot].addr = static_cast<NoAllocScratch*>(p);
+    return g_slots[slot].addr;
+}
 
 }  // namespace
 }  // namespace xjpcg
@@ -100,25 +158,23 @@ extern "C" XJPCG_Status_t xJPCG_gbSpmvDotNoAlloc(uint32_t n, const int32_t* d_ro
         d_y == nullptr || d_dot == nullptr)
         return XJPCG_STATUS_INVALID_VALUE;
     if (n > kMaxRows) return XJPCG_STATUS_INVALID_VALUE;  // scratch holds kMaxTiles partial sums
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        cudaGetLastError();
-        return XJPCG_STATUS_INTERNAL_ERROR;
-    }
     NoAllocScratch* scr = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_setupMutex);
-        if (g_scratchAddr[dev] == nullptr) {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noallocScratch) != cudaSuccess || p == nullptr) {
-                cudaGetLastError();
-                return XJPCG_STATUS_INTERNAL_ERROR;
-            }
-            g_scratchAddr[dev] = static_cast<NoAllocScratch*>(p);
-        }
-        scr = g_scratchAddr[dev];
+        scr = scratch_for_current_context();
+    }
+    if (scr == nullptr) {
+        cudaGetLastError();
+        return XJPCG_STATUS_INTERNAL_ERROR;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // The kernel's last CTA leaves the ticket at 0, so after a completed call
+    // it is already clear.  It is cleared here all the same: the array keeps
+    // whatever the previous call left, and a previous call that raced with
+    // another one (overlapping kernels on two streams, which the contract
+    // rules out but cannot prevent) can leave the ticket off by some CTAs,
+    // which would make this call's reduction finish early or never.  The
+    // clear costs one 4-byte memset on the stream and allocates nothing.
     if (cudaMemsetAsync(&scr->ticket, 0, sizeof(uint32_t), st) != cudaSuccess) {
         cudaGetLastError();
         return XJPCG_STATUS_INTERNAL_ERROR;

@@ -49,7 +49,7 @@ struct SortAcc<float> {
 __device__ __forceinline__ int sort_bin(int len) { return len > kLongRow ? 0 : 1 + (kLongRow - len); }
 
 int grid_of(int64_t work, int threads) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>((work + threads - 1) / threads, 152 * 32));
+    return (int)std::max<int64_t>(1, std::min<int64_t>((work + threads - 1) / threads, device_sm_count() * 32));
 }
 }  // namespace
 

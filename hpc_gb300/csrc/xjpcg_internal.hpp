@@ -7,6 +7,28 @@ namespace xjpcg {
 
 struct CgState;
 
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount),
+// read once per device and cached; grid-stride launches cap their grids at a
+// multiple of it.  Falls back to 1 if the query fails (the launch stays correct,
+// grid-stride loops cover the work).
+inline int device_sm_count() {
+    constexpr int kMaxDev = 64;
+    static int cache[kMaxDev] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) {
+        cudaGetLastError();
+        return 1;
+    }
+    int v = __atomic_load_n(&cache[dev], __ATOMIC_RELAXED);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    __atomic_store_n(&cache[dev], v, __ATOMIC_RELAXED);
+    return v;
+}
+
 // ---- SpMV (spmv_kernels.cu) ----
 int spmv_num_configs();
 int spmv_config_lanes(int cfg);
@@ -69,6 +91,10 @@ cudaError_t spmv_sellpat_launch(int cfg, int grid, cudaStream_t st, int n, const
 // ---- bounded-wait diagnostic (cg_kernels.cu) ----
 // out: 3 uint32 (status bits, wait duration in ns as two halves).
 cudaError_t wait_probe_launch(cudaStream_t st, uint64_t budgetNs, uint32_t* out);
+// FP64 issue-rate probe (cg_kernels.cu): out holds grid * 256 doubles.
+int fp64_rate_grid(int numSms);
+double fp64_rate_dfma(int grid, int iters);
+cudaError_t fp64_rate_launch(cudaStream_t st, int grid, int iters, double* out);
 
 // ---- length-sorted sliced SpMV (spmv_sellsort.cu) ----
 int sellsort_num_configs();

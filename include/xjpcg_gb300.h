@@ -259,6 +259,16 @@ XJPCG_Status_t xJPCG_gbSetSpmvConfig32(XJPCG_Handle_t* handle, int cfg);
 XJPCG_Status_t xJPCG_gbDiagWaitTimeout(XJPCG_Handle_t* handle, uint64_t budgetNs, uint32_t* deviceStatus,
                                        uint64_t* elapsedNs);
 
+/* FP64 issue-rate diagnostic (no counterpart in the reference).  Runs, on the
+ * handle's stream, a kernel that fills every SM with register-resident
+ * chains of FP64 fused multiply-adds (8 independent chains per thread, 2048
+ * threads per SM, iters steps per chain) and times it with CUDA events: one
+ * warm-up launch, then the best of three.  *dfmaPerSecond = DFMA instructions
+ * per second over the whole GPU, *ms = the best launch's time.  This is the
+ * FP64 ceiling the library's fp64 kernels are measured against.
+ * INVALID_VALUE for iters outside 1 .. 2^24 or null outputs. */
+XJPCG_Status_t xJPCG_gbDiagFp64Rate(XJPCG_Handle_t* handle, int32_t iters, double* dfmaPerSecond, double* ms);
+
 /* Memory-overrun diagnostic.  A handle created while the environment holds
  * XJPCG_GUARD_BYTES=N (N > 0) allocates each of its device buffers with N
  * bytes of 0xA5 after the end.  This call waits for the handle's streams and
@@ -284,9 +294,12 @@ XJPCG_Status_t xJPCG_gbDiagCheckGuards(XJPCG_Handle_t* handle, uint32_t* corrupt
  * is asynchronous on `stream` (a cudaStream_t; NULL = legacy stream), with
  * d_y and *d_dot ready when the stream reaches it.  Every call shares the
  * static array: calls whose kernels overlap on the GPU race, calls on one
- * stream do not.  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress) with that device current; make it before any stream
- * capture.  Nothing here allocates or frees. */
+ * stream do not.  The first call in a CUDA context (normally the first call
+ * on a device, in its primary context) looks up the array's address
+ * (cudaGetSymbolAddress) with that context current and caches it for that
+ * context; make it before any stream capture.  A context created later
+ * (after cudaDeviceReset, or by cuCtxCreate) gets its own lookup on its first
+ * call.  Nothing here allocates or frees. */
 XJPCG_Status_t xJPCG_gbSpmvDotNoAlloc(uint32_t n, const int32_t* d_rowPtr, const int32_t* d_colIdx,
                                       const double* d_values, const double* d_x, double* d_y, double* d_dot,
                                       void* stream);

@@ -41,9 +41,16 @@ def build() -> str:
     return LIB
 
 
-def build_ref(reference_root: str = "/root/reference") -> Optional[str]:
-    """Builds oracle/_ref/ref_partition_harness when the reference exists."""
-    if not os.path.isdir(reference_root):
+def reference_root() -> Optional[str]:
+    """The Xilinx/HPC source tree named by XJPCG_REFERENCE_ROOT, or None."""
+    root = os.environ.get("XJPCG_REFERENCE_ROOT")
+    return root if root and os.path.isdir(root) else None
+
+
+def build_ref(reference_root: Optional[str]) -> Optional[str]:
+    """Builds oracle/_ref/ref_partition_harness from the reference tree at
+    reference_root; returns None when no tree is given or it does not exist."""
+    if not reference_root or not os.path.isdir(reference_root):
         return None
     subprocess.run([os.path.join(HERE, "build_ref.sh"), reference_root], check=True, capture_output=True)
     return REF_HARNESS

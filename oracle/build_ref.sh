@@ -3,9 +3,13 @@
 # sources (Xilinx/HPC L2/sparse + utils), compiled where they lie.  Test
 # infrastructure only: the binary is used to pin the oracle's and the product's
 # format conversion and to generate the committed fixtures in tests/golden/.
-# Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
+# Usage: oracle/build_ref.sh <reference-root>   (or XJPCG_REFERENCE_ROOT set)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-$XJPCG_REFERENCE_ROOT}
+if [ -z "$REF" ]; then
+    echo "usage: $0 <reference-root> (or set XJPCG_REFERENCE_ROOT)" >&2
+    exit 2
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/L2/sparse/src/sw/c++/gen_signature.cpp" ]; then

@@ -19,7 +19,8 @@ per case, the inputs and what the reference produced:
 
 Values are data[k] = k + 1, so a stored value names the input position it
 came from.  Usage (in a container that has the reference tree):
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py <reference-root>
+(or with XJPCG_REFERENCE_ROOT set).
 """
 from __future__ import annotations
 
@@ -143,7 +144,7 @@ def _store_sig(prefix, path, rec):
                 rec[prefix + "_raw_" + f.replace(".dat", "")] = np.frombuffer(fh.read(), np.uint8)
 
 
-def run(reference_root="/root/reference"):
+def run(reference_root):
     harness = oracle.build_ref(reference_root)
     if harness is None:
         raise SystemExit("reference tree not found at %s" % reference_root)
@@ -198,4 +199,7 @@ def run(reference_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    run(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XJPCG_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit("usage: make_golden.py <reference-root> (or set XJPCG_REFERENCE_ROOT)")
+    run(root)

@@ -71,6 +71,8 @@ def test_null_handle_paths(built):
     dev, ns = C.c_uint32(0), C.c_uint64(0)
     assert lib.xJPCG_gbDiagWaitTimeout(None, 1000, C.byref(dev), C.byref(ns)) == X.NOT_INITIALIZED
     assert lib.xJPCG_gbDiagCheckGuards(None, C.byref(dev)) == X.NOT_INITIALIZED
+    r, ms = C.c_double(0.0), C.c_double(0.0)
+    assert lib.xJPCG_gbDiagFp64Rate(None, 16, C.byref(r), C.byref(ms)) == X.NOT_INITIALIZED
 
 
 def test_struct_layouts():
