@@ -14,16 +14,22 @@ the path has no data exchange).
          structure fingerprint matches), the solve and the D2H copy of x
          inside the timed region; W untimed calls first, as for value.
   roofline  the tuner's SpMV timed alone (20 launches) against the measured
-         HBM copy bandwidth, with its FP64-issue fraction; other_layouts
+         HBM copy bandwidth, with its fraction of the FP64 issue rate this
+         GPU measured in the same run (xJPCG_gbDiagFp64Rate); other_layouts
          times the int16-offset and int32-column sliced layouts the same way.
+  cpu_baseline  one complete oracle solve of the same system on all host
+         cores (rank 0, N = 1).
   extras (rank 0; --no-extras skips them): mixed vs fp64 on 160^3 and on
          the Zipf 2M system, with the FP32 SpMV's roofline; the 4,096-system
          batch in both precisions; the 96^3 adjoint; the device time of the
-         signature exporter on the bench matrix.
+         signature exporter on the bench matrix.  Each extra carries the
+         oracle's CPU time for the same work on all host cores.  A compact
+         "summary" of the extras is the line's last key.
 
 ``--impl reference`` times the oracle (the C/OpenMP restatement of the
 reference's JPCG; the reference itself only runs on an Alveo U280) on the
-host cores, on bounded samples of iterations of the same system.
+host cores: every step, warm-up included, is one complete solve of the same
+system from x0 = 0 to the same tolerance.
 """
 from __future__ import annotations
 
@@ -45,7 +51,14 @@ WORKLOAD = {"workload": "jpcg_fp64_diffusion27", "grid": "160^3", "n": 4096000, 
             "tol": 1e-10, "max_iter": 20000, "precond": "jacobi", "index": "int32", "dtype": "f64",
             "l2": "inputs larger than L2 (matrix 1.3 GB)"}
 METRIC = "fp64 JPCG time-to-1e-10 relative residual, 27-pt 160^3 (solves/s = 1/time-to-tol)"
-FP64_DFMA_PEAK = 152 * 2 * 2.07e9  # DFMA per second, nominal
+# Nominal FP64 issue rate of GB300 (1.25 TFLOP/s fp64: 2 DFMA per clock per SM
+# at 2.07 GHz on 152 SMs), reported beside the rate measured in the run.
+FP64_DFMA_NOMINAL = 152 * 2 * 2.07e9
+
+
+def bench_config(world: int) -> dict:
+    """The workload description both arms print as `config`."""
+    return dict(WORKLOAD, parallelism="replicas" if world > 1 else "single")
 
 
 def parse():
@@ -55,7 +68,6 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nx", type=int, default=160)
-    ap.add_argument("--cpu-sample-iters", type=int, default=40)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
@@ -262,16 +274,14 @@ def iter_bytes(n, nnz, col_bytes=4):
     return spmv_bytes(n, nnz, col_bytes) + 80 * n
 
 
-def cpu_sample(sysm, iters_full, sample_iters, nthreads=0):
-    """Times `sample_iters` oracle JPCG iterations on the full system."""
+def cpu_solve(sysm, tol=1e-10, max_iter=20000, nthreads=0):
+    """One complete oracle JPCG solve (x0 = 0 to tol) on the host cores:
+    (wall seconds, iterations run)."""
     import oracle
     oracle.build()
     t0 = time.perf_counter()
-    oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 20000, 1e-10, max_run=sample_iters,
-                nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    per_iter = dt / sample_iters
-    return per_iter, dt
+    r = oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, max_iter, tol, nthreads=nthreads)
+    return time.perf_counter() - t0, r["k"]
 
 
 def _timed(fn, reps=3):
@@ -288,9 +298,11 @@ def _timed(fn, reps=3):
     return float(np.median(ts)), out
 
 
-def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
+def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14, cpu_s=None):
     """fp64 JPCG and the reliable-update mixed solver on the same system, both
-    to 1e-10, with their errors against a tight FP64 oracle solve."""
+    to 1e-10, with their errors against a tight FP64 oracle solve, and the
+    oracle's fp64 time-to-tolerance on the host cores (cpu_s when the caller
+    already timed it)."""
     import torch
     import oracle
     h = X.JPCG()
@@ -315,7 +327,12 @@ def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
     gbs32 = b32 / (ms32 / 1e3) / 1e9 if ms32 > 0 else None
     tight = oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 200000, tight_tol)["x"]
     nt = np.linalg.norm(tight)
+    cpu_iters = None
+    if cpu_s is None:
+        cpu_s, cpu_iters = cpu_solve(sysm)
     out = {"system": name, "n": sysm.n, "nnz": sysm.nnz, "fp64_time_to_tol_s": t64, "fp64_iters": it64,
+           "cpu_fp64_time_to_tol_s": cpu_s, "cpu_fp64_iters": cpu_iters, "cpu_cores": oracle.max_threads(),
+           "cpu_kind": "port (oracle JPCG, one complete solve to 1e-10, all host cores)",
            "fp64_status": st64, "mixed_time_to_tol_s": tm, "mixed_fp32_iters": inf.innerIters,
            "mixed_refreshes": inf.outerSweeps, "mixed_status": m.status, "speedup": t64 / tm,
            "fp64_err_vs_oracle": float(np.linalg.norm(x64 - tight) / nt),
@@ -332,6 +349,25 @@ def mixed_vs_fp64(X, sysm, name, tight_tol=1e-14):
                                   "note": "tuner's median time of the chosen FP32 configuration"}}
     h.close()
     return out
+
+
+def cpu_batch(systems, tol=1e-10, max_iter=20000):
+    """The oracle's fp64 JPCG on every system, one system per host thread,
+    all host cores busy (ctypes releases the GIL during each solve): (wall
+    seconds, systems that met tol, threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    oracle.build()
+    threads = oracle.max_threads()
+
+    def one(s):
+        r = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, max_iter, tol, nthreads=1)
+        return int(r["status"] == 0 and r["res"] <= tol)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        ok = sum(ex.map(one, sorted(systems, key=lambda s: -s.n)))  # largest first: even finish
+    return time.perf_counter() - t0, ok, threads
 
 
 def batched_measure(X, count=4096):
@@ -357,6 +393,10 @@ def batched_measure(X, count=4096):
                     "max_err_vs_oracle_sample": err,
                     "oracle": "oracle JPCG to 1e-14 (FP64, CPU) on %d sampled systems" % len(sample)}
     h.close()
+    t_cpu, ok, threads = cpu_batch(systems)
+    out["cpu_baseline"] = {"value": count / t_cpu, "unit": "systems/s", "seconds": t_cpu, "converged": ok,
+                           "cores": threads, "kind": "port",
+                           "sample": "all %d systems, fp64 oracle JPCG to 1e-10, one system per host thread" % count}
     return out
 
 
@@ -374,9 +414,27 @@ def adjoint_measure(X, nx=96):
     ta, (st, lam, _, it, res) = _timed(lambda: h.adjoint(g, s.diag, 20000, 1e-12), 3)
     tg, _ = _timed(lambda: h.edge_grad(prob.edge_i, prob.edge_j, np.exp(prob.theta)), 3)
     h.close()
+    # The same gradient on the host cores: the oracle's forward and adjoint
+    # solves (A is symmetric) and the per-edge formula -c (l_i - l_j)(x_i - x_j).
+    import oracle
+    oracle.build()
+    c = np.exp(prob.theta)
+    t0 = time.perf_counter()
+    xf = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, prob.b, 20000, 1e-12)["x"]
+    t1 = time.perf_counter()
+    lam_c = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, xf - 0.5 * xf, 20000, 1e-12)["x"]
+    t2 = time.perf_counter()
+    _ = -c * (lam_c[prob.edge_i] - lam_c[prob.edge_j]) * (xf[prob.edge_i] - xf[prob.edge_j])
+    t3 = time.perf_counter()
     return {"grid": "%d^3" % nx, "n": n, "edges": int(prob.edge_i.size), "forward_solve_s": tf,
             "forward_iters": r.iters, "adjoint_solve_s": ta, "adjoint_iters": it, "edge_gradient_s": tg,
-            "tol": 1e-12, "note": "host-array calls (H2D/D2H inside); gradient checked in tests/test_gpu_adjoint.py"}
+            "gradient_s": tf + ta + tg,
+            "tol": 1e-12, "note": "host-array calls (H2D/D2H inside); gradient checked in tests/test_gpu_adjoint.py",
+            "cpu_baseline": {"value": t3 - t0, "unit": "s per gradient (forward + adjoint + edge gradient)",
+                             "forward_s": t1 - t0, "adjoint_s": t2 - t1, "edge_gradient_s": t3 - t2,
+                             "cores": oracle.max_threads(), "kind": "port",
+                             "sample": "one complete gradient on the %d^3 system: oracle JPCG forward and adjoint "
+                                       "solves to 1e-12 and the edge formula in numpy" % nx}}
 
 
 def export_measure(X, sysm, reps=3):
@@ -405,6 +463,34 @@ def export_measure(X, sysm, reps=3):
                                      "build host only (oracle/time_ref_partition.py), not here"}
 
 
+def summarize(line: dict) -> dict:
+    """A few numbers of the line, repeated as its last key so that a reader
+    of the line's tail sees them."""
+    r = lambda v, d=3: None if v is None else round(float(v), d)
+    s = {"solves_per_s": r(line["value"]), "e2e_solves_per_s": r((line.get("e2e") or {}).get("value")),
+         "iter_ms": r(line.get("iter_ms"), 4), "spmv_hbm_frac": r(line["roofline"]["frac"]),
+         "spmv_fp64_issue_frac": r(line["roofline"]["fp64_issue"]["frac"]),
+         "fp64_peak_gdfma_s": r(line["roofline"]["fp64_issue"]["peak_gdfma_s"], 1),
+         "cpu_solves_per_s": r((line.get("cpu_baseline") or {}).get("value"), 4)}
+    for m in line.get("mixed", []):
+        s["mixed_speedup_" + m["system"]] = r(m["speedup"])
+        s["mixed_err_" + m["system"]] = float("%.2e" % m["mixed_err_vs_oracle"])
+        s["cpu_fp64_s_" + m["system"]] = r(m.get("cpu_fp64_time_to_tol_s"))
+    b = line.get("batched")
+    if b:
+        s["batched_fp64_ms"] = r(b["fp64"]["device_ms"], 1)
+        s["batched_mixed_ms"] = r(b["mixed"]["device_ms"], 1)
+        s["batched_cpu_systems_per_s"] = r(b["cpu_baseline"]["value"], 1)
+    a = line.get("adjoint")
+    if a:
+        s["adjoint_gradient_ms"] = r(1e3 * a["gradient_s"], 1)
+        s["adjoint_cpu_gradient_ms"] = r(1e3 * a["cpu_baseline"]["value"], 1)
+    e = line.get("signature_export")
+    if e:
+        s["signature_export_ms"] = r(1e3 * e["partition_s"], 2)
+    return s
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -414,25 +500,25 @@ def run_reference(args):
     oracle.build()
     sysm = W.diffusion27(args.nx)
     threads = oracle.max_threads()
-    S = args.cpu_sample_iters
-    # Iterations to tolerance of this system: counted by the oracle itself on
-    # a full solve (untimed), so the sample converts to time-to-tolerance.
-    full = oracle.jpcg(sysm.rowptr, sysm.col, sysm.val, sysm.diag, sysm.b, 20000, 1e-10)
-    iters = full["k"]
+    # Every step, warm-up included, is one complete solve from x0 = 0 to the
+    # tolerance, so the timed region is the K solves themselves.
     for _ in range(args.warmup):
-        cpu_sample(sysm, iters, S)
-    times = [cpu_sample(sysm, iters, S)[0] for _ in range(args.steps)]
-    per_iter = float(np.median(times))
-    ttt = per_iter * iters
-    value = 1.0 / ttt
+        cpu_solve(sysm)
+    t0 = time.perf_counter()
+    steps = [cpu_solve(sysm) for _ in range(args.steps)]
+    total = time.perf_counter() - t0
+    iters = int(np.median([k for _, k in steps]))
+    ttt = total / args.steps
+    value = args.steps / total
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ttt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(WORKLOAD, parallelism="replicas"),
-            "time_to_tol_s": ttt, "iters": iters,
+            "config": bench_config(args.gpus),
+            "time_to_tol_s": ttt, "iters": iters, "step_s": [round(s, 3) for s, _ in steps],
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
-                             "sample": "%d JPCG iterations of the full 160^3 system per step, scaled by the "
-                                       "oracle's own full-solve iteration count (%d)" % (S, iters)},
+                             "sample": "%d complete solves of the 160^3 system (%d iterations each) on %d host "
+                                       "threads, %d untimed before them" % (args.steps, iters, threads,
+                                                                            args.warmup)},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -561,6 +647,11 @@ def run_gb300(args):
                                       "of which H2D of the COO arrays": inf_e.uploadMs / 1e3,
                                       "vecProc": met.m_vecProc, "solver (incl. D2H of x)": met.m_solver}}
 
+    # The FP64 issue ceiling of this GPU, measured now (register-resident DFMA
+    # chains on every SM, best of three launches): the fp64 kernels are held
+    # against it beside the HBM roofline.
+    fp64_rate, fp64_ms = h.fp64_rate()
+
     # The other sliced layouts, forced one at a time and timed the same way:
     # the tuner's choice moves the fewest bytes but is bound by FP64 issue,
     # so the layouts that carry column bytes sit higher on the HBM roofline.
@@ -586,31 +677,30 @@ def run_gb300(args):
         b_alt = spmv_bytes(n, nnz, cb_alt)
         alt_layouts.append({"layout": name_alt, "kernel": kern_alt, "launch_ms": ms_alt, "bytes_per_launch": b_alt,
                             "achieved": b_alt / (ms_alt / 1e3) / 1e9, "frac": b_alt / (ms_alt / 1e3) / 1e9 / peak,
-                            "fp64_issue_frac": nnz / (ms_alt / 1e3) / FP64_DFMA_PEAK,
+                            "fp64_issue_frac": nnz / (ms_alt / 1e3) / fp64_rate,
                             "traffic": committed_traffic(name_alt)[0]})
     h.set_spmv_lanes(0)  # back to the tuned choice
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         import oracle
-        S = args.cpu_sample_iters
-        per_iter, dt = cpu_sample(sysm, k_iters, S)
+        cpu_s, cpu_iters = cpu_solve(sysm)
         xs = np.asarray(sysm.b)
         oracle.spmv(sysm.rowptr, sysm.col, sysm.val, xs)
         t0 = time.perf_counter()
         for _ in range(5):
             oracle.spmv(sysm.rowptr, sysm.col, sysm.val, xs)
         spmv_cpu_s = (time.perf_counter() - t0) / 5
-        cpu = {"value": 1.0 / (per_iter * k_iters), "unit": "solves/s", "cores": oracle.max_threads(),
+        cpu = {"value": 1.0 / cpu_s, "unit": "solves/s", "cores": oracle.max_threads(),
                "kind": "port", "spmv_gbs": spmv_bytes(n, nnz) / spmv_cpu_s / 1e9,
                "spmv_note": "oracle CSR SpMV (12 B per entry), all host cores, 5 launches",
-               "sample": "%d oracle JPCG iterations on the full 160^3 system (%.1f s), scaled to the %d "
-                         "iterations of the GPU solve" % (S, dt, k_iters)}
+               "sample": "one complete oracle JPCG solve of the 160^3 system to 1e-10 (%.2f s, %d iterations) "
+                         "on all host cores" % (cpu_s, cpu_iters)}
 
     extras = {}
     if rank == 0 and not args.no_extras:
         from hpc_gb300 import workloads as W
-        extras["mixed"] = [mixed_vs_fp64(X, sysm, "diffusion27_160"),
+        extras["mixed"] = [mixed_vs_fp64(X, sysm, "diffusion27_160", cpu_s=(1.0 / cpu["value"] if cpu else None)),
                            mixed_vs_fp64(X, W.zipf_spd(2_000_000, seed=2), "zipf_spd_2M")]
         extras["batched"] = batched_measure(X)
         extras["adjoint"] = adjoint_measure(X)
@@ -620,9 +710,9 @@ def run_gb300(args):
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ttt * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single",
-                               spmv_lanes=info.spmvLanes, spmv_grid=info.spmvGrid,
-                               spmv_tuning=[list(t) for t in tuning]),
+                "config": bench_config(world),
+                "spmv_choice": {"lanes": info.spmvLanes, "grid": info.spmvGrid, "cfg": info.spmvCfg,
+                                "tuning": [list(t) for t in tuning]},
                 "time_to_tol_s": ttt, "iters": k_iters, "iter_ms": iter_ms, "iter_gbs": iter_gbs,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
@@ -632,15 +722,19 @@ def run_gb300(args):
                              "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                              "traffic_source": traffic_src,
                              "fp64_issue": {"achieved_gdfma_s": nnz / (spmv_ms / 1e3) / 1e9,
-                                            "peak_gdfma_s": FP64_DFMA_PEAK / 1e9,
-                                            "frac": nnz / (spmv_ms / 1e3) / FP64_DFMA_PEAK,
-                                            "note": "one DFMA per stored entry; peak = nominal 1.25 TFLOP/s fp64 "
-                                                    "(2 DFMA per clock per SM, 152 SMs, 2.07 GHz). The SpMV is "
-                                                    "bound by whichever fraction is higher"},
+                                            "peak_gdfma_s": fp64_rate / 1e9,
+                                            "frac": nnz / (spmv_ms / 1e3) / fp64_rate,
+                                            "peak_source": "measured in this run (xJPCG_gbDiagFp64Rate: "
+                                                           "register-resident DFMA chains on every SM, "
+                                                           "%.2f ms best of 3)" % fp64_ms,
+                                            "nominal_gdfma_s": FP64_DFMA_NOMINAL / 1e9,
+                                            "note": "one DFMA per stored entry; the SpMV is bound by whichever "
+                                                    "fraction is higher"},
                              "other_layouts": alt_layouts},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clock_info,
                 "loop": "conditional-graph" if h.info().loopMode == 1 else "host"}
         line.update(extras)
+        line["summary"] = summarize(line)
         print(json.dumps(line), flush=True)
     h.close()
     if world > 1:

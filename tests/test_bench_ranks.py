@@ -56,8 +56,7 @@ def test_reference_arm_two_ranks():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--nx", "16",
-           "--cpu-sample-iters", "4"]
+           "--impl", "reference", "--gpus", "2", "--steps", "2", "--warmup", "1", "--nx", "16"]
     out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
@@ -65,3 +64,9 @@ def test_reference_arm_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    # every step is a complete solve: the timed region is the steps themselves
+    assert d["steps"] == 2 and d["warmup"] == 1 and len(d["step_s"]) == 2
+    assert abs(d["ms_per_step"] / 1e3 - sum(d["step_s"]) / 2) < 0.05 * d["ms_per_step"] / 1e3 + 0.01
+    # the config both arms print, for N = 2 replicas
+    import bench
+    assert d["config"] == json.loads(json.dumps(bench.bench_config(2)))
