@@ -39,7 +39,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbGetSpmvTuning", "xJPCG_gbSpmvDotNoAlloc", "xJPCG_gbBatchSolve",
     "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv", "xJPCG_gbSetSignatureSumOrder",
     "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32", "xJPCG_gbDiagWaitTimeout",
-    "xJPCG_gbDiagCheckGuards", "xJPCG_gbDiagFp64Rate",
+    "xJPCG_gbDiagCheckGuards", "xJPCG_gbDiagFp64Rate", "xJPCG_gbCreateHandleOnDevice", "xJPCG_gbStoreYFrames",
 ]
 
 
@@ -125,6 +125,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbDiagWaitTimeout.argtypes = [_P, u64, C.POINTER(u32), C.POINTER(u64)]
     lib.xJPCG_gbDiagCheckGuards.argtypes = [_P, C.POINTER(u32)]
     lib.xJPCG_gbDiagFp64Rate.argtypes = [_P, C.c_int32, C.POINTER(dbl), C.POINTER(dbl)]
+    lib.xJPCG_gbCreateHandleOnDevice.argtypes = [C.POINTER(_P), C.c_int, C.c_char_p]
+    lib.xJPCG_gbStoreYFrames.argtypes = [_P, u64, u32, _P, u64, C.POINTER(u64)]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbGetSpmvTuning32.argtypes = [_P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
@@ -149,6 +151,17 @@ def spmv_dot_no_alloc(n: int, d_rowptr: int, d_col: int, d_val: int, d_x: int, d
     """xJPCG_gbSpmvDotNoAlloc: y = A x and x.y on caller-owned device memory,
     with no device allocation (see include/xjpcg_gb300.h).  Returns the status."""
     return load().xJPCG_gbSpmvDotNoAlloc(n, d_rowptr, d_col, d_val, d_x, d_y, d_dot, stream or None)
+
+
+def store_y_frames(frames: bytes, num_nodes: int, y) -> tuple:
+    """xJPCG_gbStoreYFrames: writes num_nodes transY frames into the float64
+    array y in place (host only).  Returns (status, bytes of frames read)."""
+    buf = np.frombuffer(bytes(frames), np.uint8)
+    assert y.dtype == np.float64 and y.flags["C_CONTIGUOUS"]
+    used = C.c_uint64(0)
+    st = load().xJPCG_gbStoreYFrames(buf.ctypes.data if buf.size else None, buf.size, num_nodes,
+                                     y.ctypes.data, y.nbytes, C.byref(used))
+    return st, used.value
 
 
 def error_string(code: int) -> str:
@@ -178,10 +191,13 @@ class JPCG:
     outputs, and never raises for a solver status (check ``.status``).
     """
 
-    def __init__(self, xclbin: str = ""):
+    def __init__(self, xclbin: str = "", device: Optional[int] = None):
         self.lib = load()
         self.h = _P()
-        st = self.lib.xJPCG_createHandle(C.byref(self.h), xclbin.encode())
+        if device is None:
+            st = self.lib.xJPCG_createHandle(C.byref(self.h), xclbin.encode())
+        else:
+            st = self.lib.xJPCG_gbCreateHandleOnDevice(C.byref(self.h), device, xclbin.encode())
         if st != SUCCESS:
             msg = self.last_message()
             raise XJPCGError(st, msg)

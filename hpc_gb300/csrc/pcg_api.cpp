@@ -27,6 +27,27 @@ double elapsed(std::chrono::time_point<std::chrono::high_resolution_clock>& last
 PcgHandle* impl(XJPCG_Handle_t* h) { return reinterpret_cast<PcgHandle*>(h); }
 const PcgHandle* impl(const XJPCG_Handle_t* h) { return reinterpret_cast<const PcgHandle*>(h); }
 
+// Makes the handle's device current for one API call and gives the calling
+// thread its previous device back afterwards, so that a handle created on
+// one device keeps working whatever device the caller has current.
+class DeviceScope {
+   public:
+    explicit DeviceScope(const PcgHandle* p) {
+        if (p == nullptr || !p->initDone()) return;
+        if (cudaGetDevice(&m_prev) == cudaSuccess && m_prev != p->device() && cudaSetDevice(p->device()) == cudaSuccess)
+            m_switched = true;
+    }
+    ~DeviceScope() {
+        if (m_switched) cudaSetDevice(m_prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+
+   private:
+    int m_prev = 0;
+    bool m_switched = false;
+};
+
 // The index base of a mode; the reference rejects anything but 0 and 1 in
 // SparseMatrix::loadCoo / loadCscSym (matrix_params.hpp:51-60, 82-96) with an
 // SpmNotSupported exception that surfaces as INTERNAL_ERROR.
@@ -58,14 +79,26 @@ void finishSolve(PcgHandle* p, const xjpcg::Results& r, double tol, double* res,
 extern "C" {
 
 XJPCG_Status_t xJPCG_createHandle(XJPCG_Handle_t** handle, const char* xclbinPath) {
+    return xJPCG_gbCreateHandleOnDevice(handle, -1, xclbinPath);
+}
+
+XJPCG_Status_t xJPCG_gbCreateHandleOnDevice(XJPCG_Handle_t** handle, int deviceId, const char* xclbinPath) {
     (void)xclbinPath;
     if (handle == nullptr) return XJPCG_STATUS_INVALID_VALUE;
     PcgHandle* p = new (std::nothrow) PcgHandle();
     if (p == nullptr) return XJPCG_STATUS_ALLOC_FAILED;
     *handle = reinterpret_cast<XJPCG_Handle_t*>(p);
+    int prev = -1;
+    if (deviceId >= 0 && cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    struct Restore {
+        int dev;
+        ~Restore() {
+            if (dev >= 0) cudaSetDevice(dev);
+        }
+    } restore{prev};
     try {
         auto last = std::chrono::high_resolution_clock::now();
-        p->init();
+        p->init(deviceId);
         p->metrics()->m_objInit = elapsed(last);
     } catch (const CgError& e) {
         return p->setStatusMessage(e.status, e.what());
@@ -77,6 +110,7 @@ XJPCG_Status_t xJPCG_createHandle(XJPCG_Handle_t** handle, const char* xclbinPat
 
 XJPCG_Status_t xJPCG_destroyHandle(XJPCG_Handle_t* handle) {
     if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED;
+    DeviceScope scope(impl(handle));
     delete impl(handle);
     return XJPCG_STATUS_SUCCESS;
 }
@@ -224,6 +258,7 @@ const char* xJPCG_getErrorString(const XJPCG_Status_t code) {
 #define XJ_GUARD_BEGIN                                 \
     if (handle == nullptr) return XJPCG_STATUS_NOT_INITIALIZED; \
     PcgHandle* p = impl(handle);                        \
+    DeviceScope deviceScope_(p);                        \
     try {
 #define XJ_GUARD_END(msg)                                               \
     }                                                                   \
@@ -478,6 +513,38 @@ XJPCG_Status_t xJPCG_gbDiagCheckGuards(XJPCG_Handle_t* handle, uint32_t* corrupt
     *corrupted = p->checkGuards(&first);
     if (*corrupted) throw xjpcg::InternalError("a kernel wrote past the end of " + first);
     XJ_GUARD_END("Guard bytes intact")
+}
+
+// The receiving side of the dSpmv transY framing, as dStoreY writes it
+// (dSpmv/hw/include/impl/dStoreY.hpp:36-65): for each of numNodes frames, a
+// 64-byte header word {startAddr, rows, ...} (uint32, startAddr counted in
+// 32-byte memory words), then ceil(rows / 8) 64-byte data words, each stored
+// as two 32-byte memory words at startAddr, startAddr + 1, ...  Every data
+// word is written whole, so the zero fill of a last partial word lands in y
+// too, as on the FPGA.  Host memory only; no device work.
+XJPCG_Status_t xJPCG_gbStoreYFrames(const void* frames, uint64_t frameBytes, uint32_t numNodes, double* y,
+                                    uint64_t yBytes, uint64_t* consumedBytes) {
+    if (frames == nullptr || y == nullptr) return XJPCG_STATUS_INVALID_VALUE;
+    const unsigned char* in = static_cast<const unsigned char*>(frames);
+    unsigned char* out = reinterpret_cast<unsigned char*>(y);
+    uint64_t pos = 0;
+    for (uint32_t node = 0; node < numNodes; ++node) {
+        if (pos > frameBytes || frameBytes - pos < 64) return XJPCG_STATUS_INVALID_VALUE;
+        uint32_t head[2];
+        std::memcpy(head, in + pos, sizeof(head));
+        const uint64_t startByte = (uint64_t)head[0] * 32u;
+        const uint64_t words = ((uint64_t)head[1] + 7u) / 8u;
+        // rows = 0: transY still emits one data word that dStoreY never
+        // reads, which would shift every later frame; refused instead.
+        if (head[1] == 0) return XJPCG_STATUS_INVALID_VALUE;
+        if (frameBytes - pos - 64 < words * 64) return XJPCG_STATUS_INVALID_VALUE;
+        if (startByte > yBytes || yBytes - startByte < words * 64) return XJPCG_STATUS_INVALID_VALUE;
+        std::memcpy(out + startByte, in + pos + 64, words * 64);
+        pos += 64 + words * 64;
+        if (consumedBytes) *consumedBytes = pos;
+    }
+    if (consumedBytes) *consumedBytes = pos;
+    return XJPCG_STATUS_SUCCESS;
 }
 
 }  // extern "C"

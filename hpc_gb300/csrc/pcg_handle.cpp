@@ -129,8 +129,9 @@ void PcgHandle::faultPoint(const char* what) {
     if (m_faultLaunch) check(cudaErrorLaunchFailure, what);
 }
 
-void PcgHandle::init() {
+void PcgHandle::init(int device) {
     m_guardBytes = (size_t)std::max(0, envInt("XJPCG_GUARD_BYTES", 0));
+    if (device >= 0) check(cudaSetDevice(device), "cudaSetDevice");
     check(cudaGetDevice(&m_device), "cudaGetDevice");
     check(cudaDeviceGetAttribute(&m_numSms, cudaDevAttrMultiProcessorCount, m_device), "cudaDeviceGetAttribute");
     check(cudaStreamCreateWithFlags(&m_stream, cudaStreamNonBlocking), "cudaStreamCreate");

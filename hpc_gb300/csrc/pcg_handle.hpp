@@ -97,7 +97,10 @@ class PcgHandle {
    public:
     PcgHandle() = default;
     ~PcgHandle();
-    void init();
+    // device < 0: the calling thread's current device.
+    void init(int device = -1);
+    bool initDone() const { return m_initDone; }
+    int device() const { return m_device; }
 
     // Matrix input.  base: 0 = C, 1 = Fortran (mode >> 4).
     void setCooMat(uint32_t n, uint64_t nnz, const uint32_t* row, const uint32_t* col, const double* data, int base);

@@ -58,6 +58,14 @@ typedef struct {
     double res;        /* fp64: sqrt(r.r / b.b) of the recursive residual; mixed: true relative residual */
 } XJPCG_GbBatchResult_t;
 
+/* xJPCG_createHandle on a chosen CUDA device (no counterpart in pcg.h; the
+ * reference selects its card through the FPGA object's setId,
+ * L2/common/include/sw/xNativeFPGA.hpp).  deviceId < 0 takes the calling
+ * thread's current device, as xJPCG_createHandle does.  The caller's current
+ * device is the same after the call as before it.  Every call on the handle
+ * runs on its device and leaves the caller's current device unchanged. */
+XJPCG_Status_t xJPCG_gbCreateHandleOnDevice(XJPCG_Handle_t** handle, int deviceId, const char* xclbinPath);
+
 /* CSR input (0- or 1-based per the mode's index nibble), same contract as
  * xJPCG_cooSolver otherwise.  The row pointer and column arrays are int32.
  * New symbol; pcg.h:178-215 is the COO form it parallels. */
@@ -135,6 +143,22 @@ XJPCG_Status_t xJPCG_gbGetSignature(XJPCG_Handle_t* handle, void* rbParam, void*
  * >= 64 + 64 * max(1, ceil(yRows / 8)). */
 XJPCG_Status_t xJPCG_gbSignatureSpmv(XJPCG_Handle_t* handle, const double* x, uint32_t xLen, double* y,
                                      uint32_t yRows, uint32_t startAddr, void* frame, uint64_t frameBytes);
+
+/* dSpmv store side (replaces dSpmvStoreYhost::run + getY,
+ * dSpmv/sw/include/dSpmvStoreYhost.hpp:27-55, and the krnl_dStoreY kernel,
+ * dSpmv/hw/include/impl/dStoreY.hpp:36-65).  Reads numNodes transY frames
+ * back to back from `frames` (frameBytes bytes, host memory) and writes each
+ * into y as dStoreY does: a 64-byte header word {startAddr, rows, ...}
+ * (uint32; startAddr counted in 32-byte memory words), then ceil(rows / 8)
+ * 64-byte data words, stored whole from byte 32 * startAddr on, so a last
+ * partial word's zero fill is written too.  No handle and no device work.
+ * INVALID_VALUE for a null pointer, a frame that runs past frameBytes, a
+ * frame that would write past yBytes, or a header with rows = 0 (the transY
+ * kernel still emits one data word for it, which dStoreY would not read, so
+ * every later frame would be misread); frames before the bad one are
+ * written.  *consumedBytes (may be NULL) = bytes of frames read. */
+XJPCG_Status_t xJPCG_gbStoreYFrames(const void* frames, uint64_t frameBytes, uint32_t numNodes, double* y,
+                                    uint64_t yBytes, uint64_t* consumedBytes);
 
 /* Summation order of xJPCG_gbSignatureSpmv.  0 (the default): the tuned SpMV
  * kernels, each row summed in its CSR order with fused multiply-adds.
