@@ -72,11 +72,13 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the mixed-precision, batched and adjoint measurements")
-    ap.add_argument("--profile", choices=["spmv", "solve", "mixed", "batched", "adjoint", "export"], default=None,
+    ap.add_argument("--profile", choices=["spmv", "solve", "mixed", "batched", "adjoint", "export", "fp64"],
+                    default=None,
                     help="profiling driver for ncu: set the matrix, then run --reps plain SpMVs "
                          "(spmv), one resident fp64 solve (solve) or one mixed solve (mixed); or one batched "
                          "solve of --systems systems (batched); or the adjoint solve and gradients on "
-                         "--nx^3 (adjoint); or the signature export of the matrix (export); no timing line")
+                         "--nx^3 (adjoint); or the signature export of the matrix (export); or the FP64 "
+                         "issue-rate probe at several lengths (fp64, prints its rates); no timing line")
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--workload", choices=["diffusion27", "zipf"], default="diffusion27",
                     help="matrix of --profile: diffusion27(--nx) or the 2M-row Zipf SPD system")
@@ -201,6 +203,12 @@ def run_profile(args):
     import torch
     import hpc_gb300 as X
     from hpc_gb300 import workloads as W
+    if args.profile == "fp64":
+        with X.JPCG() as h:
+            for iters in (4096, 16384, 65536):
+                rate, ms = h.fp64_rate(iters)
+                print("fp64 probe iters=%d: %.3f ms, %.1f G DFMA/s" % (iters, ms, rate / 1e9), flush=True)
+        return
     if args.profile == "batched":
         systems = W.batched_stencils(count=args.systems, seed=3)
         h = X.JPCG()

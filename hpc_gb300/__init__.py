@@ -40,6 +40,7 @@ EXPORTED_SYMBOLS = [
     "xJPCG_gbAdjointSolve", "xJPCG_gbEdgeGrad", "xJPCG_gbSetSignatureMatrix", "xJPCG_gbSignatureSpmv", "xJPCG_gbSetSignatureSumOrder",
     "xJPCG_gbExportSignature", "xJPCG_gbGetSignature", "xJPCG_gbGetSpmvTuning32", "xJPCG_gbDiagWaitTimeout",
     "xJPCG_gbDiagCheckGuards", "xJPCG_gbDiagFp64Rate", "xJPCG_gbCreateHandleOnDevice", "xJPCG_gbStoreYFrames",
+    "xJPCG_gbSignatureSolve",
 ]
 
 
@@ -127,6 +128,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.xJPCG_gbDiagFp64Rate.argtypes = [_P, C.c_int32, C.POINTER(dbl), C.POINTER(dbl)]
     lib.xJPCG_gbCreateHandleOnDevice.argtypes = [C.POINTER(_P), C.c_int, C.c_char_p]
     lib.xJPCG_gbStoreYFrames.argtypes = [_P, u64, u32, _P, u64, C.POINTER(u64)]
+    lib.xJPCG_gbSignatureSolve.argtypes = [_P, u32, _P, _P, _P, u32, dbl, C.POINTER(u32), C.POINTER(dbl)]
     lib.xJPCG_gbGetSpmvTuning.argtypes = [_P, _P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbGetSpmvTuning32.argtypes = [_P, _P, C.c_int32, C.POINTER(C.c_int32)]
     lib.xJPCG_gbSpmvDotNoAlloc.argtypes = [u32, _P, _P, _P, _P, _P, _P, _P]
@@ -389,6 +391,18 @@ class JPCG:
         if st != SUCCESS:
             raise XJPCGError(st, self.last_message())
         return (y, fr) if frame else y
+
+    def signature_solve(self, b, diag, max_iter, tol):
+        """JPCG on the partitioned matrix (xJPCG_gbSignatureSolve); with sum
+        order 1, in the reference FPGA's arithmetic order.  Returns a result
+        with status, x, iters, res and message."""
+        b = np.ascontiguousarray(b, np.float64)
+        diag = np.ascontiguousarray(diag, np.float64)
+        x = np.zeros(b.size, np.float64)
+        it, res = C.c_uint32(0), C.c_double(0.0)
+        st = self.lib.xJPCG_gbSignatureSolve(self.h, b.size, _ptr(b), _ptr(diag), _ptr(x), max_iter, tol,
+                                             C.byref(it), C.byref(res))
+        return SolveResult(st, x, it.value, res.value, self.last_message())
 
     def export_signature(self) -> dict:
         """The stored matrix in the reference's partitioned format:

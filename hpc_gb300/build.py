@@ -28,7 +28,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
            "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
 SOURCES = ["spmv_kernels.cu", "spmv_sellpat.cu", "spmv_sellsort.cu", "spmv_merge.cu", "cg_kernels.cu", "mixed_kernels.cu", "convert_kernels.cu",
-           "spmv_noalloc.cu", "batched_kernels.cu", "adjoint_kernels.cu", "signature_kernels.cu", "signature_export.cu", "pcg_handle.cpp", "pcg_api.cpp"]
+           "spmv_noalloc.cu", "batched_kernels.cu", "adjoint_kernels.cu", "signature_kernels.cu", "signature_export.cu", "fpga_order.cu", "pcg_handle.cpp", "pcg_api.cpp"]
 HEADERS = ["xjpcg_device.cuh", "xjpcg_state.h", "xjpcg_internal.hpp", "pcg_handle.hpp"]
 
 

@@ -238,9 +238,15 @@ cudaError_t wait_probe_launch(cudaStream_t st, uint64_t budgetNs, uint32_t* out)
 // cover the pipe's latency at full occupancy), so the kernel issues nothing
 // but DFMA once its few loads are done.  m < 1 keeps the chains finite; one
 // store of their sum per thread keeps the compiler from removing them.
+// m and c are computed per thread so that they live in registers, as the
+// operands of the library's own FMAs do: a DFMA that reads an operand from
+// the constant bank (a kernel parameter) issued at about 5/6 of this rate
+// when measured on GB300.
 constexpr int kFp64Chains = 8;
 
-__global__ void __launch_bounds__(kVecThreads) fp64_rate_kernel(int iters, double m, double c, double* out) {
+__global__ void __launch_bounds__(kVecThreads) fp64_rate_kernel(int iters, double m0, double c0, double* out) {
+    const double m = m0 - 1e-12 * (double)(threadIdx.x & 31);
+    const double c = c0 * (double)((threadIdx.x & 7) + 1);
     double a[kFp64Chains];
 #pragma unroll
     for (int j = 0; j < kFp64Chains; ++j) a[j] = (double)(threadIdx.x + j) * 1e-3;

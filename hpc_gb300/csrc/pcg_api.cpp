@@ -361,6 +361,18 @@ XJPCG_Status_t xJPCG_gbSignatureSpmv(XJPCG_Handle_t* handle, const double* x, ui
     XJ_GUARD_END("SpMV returns successfully")
 }
 
+XJPCG_Status_t xJPCG_gbSignatureSolve(XJPCG_Handle_t* handle, uint32_t n, const double* b, const double* diagA,
+                                      double* x, uint32_t maxIter, double tol, uint32_t* iter, double* res) {
+    XJ_GUARD_BEGIN
+    auto last = std::chrono::high_resolution_clock::now();
+    if (iter == nullptr || res == nullptr) throw xjpcg::InvalidValue("iter and res must not be null.");
+    p->metrics()->m_matProc = 0.0;
+    p->metrics()->m_vecProc = 0.0;
+    xjpcg::Results r = p->signatureSolve(n, b, diagA, x, maxIter, tol);
+    finishSolve(p, r, tol, res, iter, nullptr, last);
+    XJ_GUARD_END("Solver returns successfully")
+}
+
 XJPCG_Status_t xJPCG_gbSetSignatureSumOrder(XJPCG_Handle_t* handle, int order) {
     XJ_GUARD_BEGIN
     p->setSignatureSumOrder(order);

@@ -1442,6 +1442,79 @@ void PcgHandle::setSignatureSumOrder(int order) {
     m_sigSumOrder = order;
 }
 
+// JPCG over the matrix loaded by setSignatureMatrix.  Order 1: the loop of
+// fpga_order.cu, driven from the host in batches of 8 iterations (each
+// kernel that changes the solve returns at once when the loop is done).
+// Order 0: the tuned solve on the decoded CSR, with b and diag padded to the
+// matrix size (b 0, diag 1), as the 4-padding of cgVector.hpp:67-73 does.
+Results PcgHandle::signatureSolve(uint32_t n, const double* b, const double* diag, double* x, uint32_t maxIter,
+                                  double tol) {
+    Range range_("xJPCG signature solve");
+    if (b == nullptr || diag == nullptr) throw InvalidValue("Vector is nullptr.");
+    if (!m_haveMatrix || m_kind != 4) throw InvalidValue("no matrix loaded by xJPCG_gbSetSignatureMatrix.");
+    const uint32_t n4 = (n + 3) / 4 * 4;
+    if (n == 0 || n > m_n || n4 > m_n4) throw InvalidValue("vector dimension exceeds the partitioned matrix.");
+    if (m_sigSumOrder == 0) {
+        std::vector<double> bp(m_n, 0.0), dp(m_n, 1.0);
+        std::copy(b, b + n, bp.begin());
+        std::copy(diag, diag + n, dp.begin());
+        setVec(m_n, bp.data(), dp.data(), false);
+        Results r = run(maxIter, tol);
+        if (x) copyX(x, n, false);
+        return r;
+    }
+    if (m_sigOrderedGen != m_valGen)
+        throw InvalidValue("the reference-order solve needs a matrix loaded by xJPCG_gbSetSignatureMatrix and "
+                           "unchanged since.");
+    const uint64_t want = std::min<uint64_t>((uint64_t)maxIter + 2, kMaxRecords);
+    if (want > m_recCap) {
+        alloc(m_records, sizeof(IterRecord) * want, "iteration records");
+        m_recCap = want;
+    }
+    check(cudaMemsetAsync(m_records.p, 0, sizeof(IterRecord) * want, m_stream), "memset records");
+    CgState cmd = {};
+    cmd.tol = tol;
+    cmd.maxIterP1 = maxIter + 1u;
+    cmd.records = m_records.as<IterRecord>();
+    cmd.recCap = (uint32_t)want;
+    CgState* st = m_state.as<CgState>();
+    check(cudaMemcpyAsync(st, &cmd, sizeof(CgState), cudaMemcpyHostToDevice, m_stream), "state upload");
+    const size_t vb = sizeof(double) * ((size_t)m_n4 + 4);
+    check(cudaMemsetAsync(m_p.p, 0, vb, m_stream), "memset p");  // p past n4 stays 0 for the SpMV's gathers
+    check(cudaMemsetAsync(m_Ap.p, 0, vb, m_stream), "memset Ap");
+    check(cudaMemcpyAsync(m_b.p, b, sizeof(double) * n, cudaMemcpyHostToDevice, m_stream), "H2D b");
+    check(cudaMemcpyAsync(m_diag.p, diag, sizeof(double) * n, cudaMemcpyHostToDevice, m_stream), "H2D diag");
+    alloc(m_foPart, sizeof(double) * (2 * (size_t)fo_blocks((int)n4) + 2), "reference-order dot blocks");
+    faultPoint("reference-order solve");
+    check(cudaEventRecord(m_ev0, m_stream), "event");
+    check(fo_init(m_stream, (int)n, (int)n4, m_b.as<double>(), m_diag.as<double>(), m_x.as<double>(),
+                  m_r.as<double>(), m_p.as<double>(), m_J.as<double>(), m_Ap.as<double>(), st),
+          "reference-order init");
+    uint64_t ran = 0;
+    for (;;) {
+        for (int u = 0; u < 8; ++u) {
+            check(sig_ordered_spmv(m_stream, (int)m_n, m_sigRunPtr.as<int>(), m_sigRunList.as<int>(),
+                                   m_sigVal.as<double>(), m_sigCol.as<uint32_t>(), m_p.as<double>(),
+                                   m_Ap.as<double>()),
+                  "reference-order SpMV");
+            check(fo_iteration_tail(m_stream, (int)n4, m_x.as<double>(), m_p.as<double>(), m_r.as<double>(),
+                                    m_Ap.as<double>(), m_J.as<double>(), m_foPart.as<double>(), st),
+                  "reference-order iteration");
+        }
+        ran += 8;
+        uint32_t done = 0;
+        check(cudaMemcpyAsync(&done, &st->done, sizeof(uint32_t), cudaMemcpyDeviceToHost, m_stream), "D2H");
+        check(cudaStreamSynchronize(m_stream), "sync");
+        if (done || ran > (uint64_t)maxIter + 1) break;
+    }
+    check(cudaEventRecord(m_ev1, m_stream), "event");
+    check(cudaMemcpyAsync(&m_lastState, st, sizeof(CgState), cudaMemcpyDeviceToHost, m_stream), "state download");
+    if (x) check(cudaMemcpyAsync(x, m_x.p, sizeof(double) * n, cudaMemcpyDeviceToHost, m_stream), "D2H x");
+    check(cudaStreamSynchronize(m_stream), "sync");
+    check(cudaEventElapsedTime(&m_lastMs, m_ev0, m_ev1), "event");
+    return readResults(maxIter);
+}
+
 void PcgHandle::signatureSpmv(const double* x, uint32_t xLen, double* y, uint32_t yRows, uint32_t startAddr,
                               unsigned char* frame, uint64_t frameBytes) {
     if (!m_haveMatrix) throw InvalidValue("no matrix has been set.");

@@ -125,6 +125,10 @@ class PcgHandle {
     void setSignatureMatrix(uint32_t nch, const void* const* bufs, const uint64_t* bytes, const void* par,
                             uint64_t parBytes, const void* rb, uint64_t rbBytes);
     void setSignatureSumOrder(int order);
+    // JPCG on the leading n x n block of the signature matrix: summation
+    // order 1 = the reference FPGA's arithmetic order (fpga_order.cu), 0 =
+    // the tuned solver on the decoded CSR.  Host arrays.
+    Results signatureSolve(uint32_t n, const double* b, const double* diag, double* x, uint32_t maxIter, double tol);
     void signatureSpmv(const double* x, uint32_t xLen, double* y, uint32_t yRows, uint32_t startAddr,
                        unsigned char* frame, uint64_t frameBytes);
     uint32_t sigRows() const { return m_sigRows; }
@@ -288,6 +292,7 @@ class PcgHandle {
     int m_sigSumOrder = 0;                         // 0 = fastest SpMV, 1 = the reference's summation order
     uint64_t m_valGen = 0, m_sigOrderedGen = ~0ull;  // matrix values generation; the one the run lists match
     SigExport m_sigExport;
+    DevBuf m_foPart;  // block sums of the reference-order dots
     uint64_t m_structGen = 0;  // bumped whenever a new matrix structure is stored
     // adjoint
     DevBuf m_xKeep, m_lambda, m_grad, m_edgeI, m_edgeJ, m_edgeC, m_edgeG;

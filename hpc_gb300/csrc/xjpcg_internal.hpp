@@ -91,6 +91,13 @@ cudaError_t spmv_sellpat_launch(int cfg, int grid, cudaStream_t st, int n, const
 // ---- bounded-wait diagnostic (cg_kernels.cu) ----
 // out: 3 uint32 (status bits, wait duration in ns as two halves).
 cudaError_t wait_probe_launch(cudaStream_t st, uint64_t budgetNs, uint32_t* out);
+// The JPCG loop in the reference FPGA's arithmetic order (fpga_order.cu).
+// z is written over Ap (Apz); t holds 2 * fo_blocks(n4) doubles.
+int fo_blocks(int n4);
+cudaError_t fo_init(cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x, double* r,
+                    double* p, double* J, double* z, CgState* s);
+cudaError_t fo_iteration_tail(cudaStream_t st, int n4, double* x, double* p, double* r, double* Apz, const double* J,
+                              double* t, CgState* s);
 // FP64 issue-rate probe (cg_kernels.cu): out holds grid * 256 doubles.
 int fp64_rate_grid(int numSms);
 double fp64_rate_dfma(int grid, int iters);

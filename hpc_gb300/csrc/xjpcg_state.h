@@ -48,6 +48,7 @@ struct alignas(16) CgState {
     uint64_t relHandle;            // mixed precision: conditional handle of the refresh
     uint32_t skipRefresh;          // mixed precision: 1 = the refresh kernels of this iteration return at once
     uint32_t xSkip;                // fp64: 1 = the update kernel found the loop done (no x update due)
+    uint32_t pupdateDue;           // reference-order loop: 1 = this iteration's p update is due
 };
 
 }  // namespace xjpcg

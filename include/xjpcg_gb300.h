@@ -144,6 +144,26 @@ XJPCG_Status_t xJPCG_gbGetSignature(XJPCG_Handle_t* handle, void* rbParam, void*
 XJPCG_Status_t xJPCG_gbSignatureSpmv(XJPCG_Handle_t* handle, const double* x, uint32_t xLen, double* y,
                                      uint32_t yRows, uint32_t startAddr, void* frame, uint64_t frameBytes);
 
+/* JPCG on the matrix loaded by xJPCG_gbSetSignatureMatrix (the reference's
+ * partitioned buffers), leading n x n block; b, diagA and x are host arrays
+ * of n entries; same stop rule, counters, records and status as
+ * xJPCG_cooSolver.  With summation order 1 (xJPCG_gbSetSignatureSumOrder)
+ * every operation of the loop follows the reference FPGA's arithmetic as its
+ * C source states it: the vector init of pcg/sw/include/impl/cgVector.hpp:
+ * 101-114 (bb and r.z summed in index order), the SpMV order of
+ * xJPCG_gbSignatureSpmv, the dot products of xf::blas::DotHelper<double, 2>
+ * and nrm2s (L1/blas/include/hw/blas/helpers/funcs/dotHelper.hpp, sum.hpp:
+ * 4-entry trees, zero-padded 8-entry trees, then the 8-entry sums added in
+ * order), the axpy updates x = alpha*p + x, r = (-alpha)*Ap + r,
+ * p = beta*p + z and z = r*J, each multiply, add and divide rounded on its
+ * own.  The records and x are then the bits a C execution of that source
+ * gives (a checking mode: its dot sums run on one thread).  With order 0 it
+ * is the tuned solver on the decoded matrix, b and diag padded to the matrix
+ * size with 0 and 1.  INVALID_VALUE when no partitioned matrix is loaded (or,
+ * for order 1, it changed since) or n exceeds it. */
+XJPCG_Status_t xJPCG_gbSignatureSolve(XJPCG_Handle_t* handle, uint32_t n, const double* b, const double* diagA,
+                                      double* x, uint32_t maxIter, double tol, uint32_t* iter, double* res);
+
 /* dSpmv store side (replaces dSpmvStoreYhost::run + getY,
  * dSpmv/sw/include/dSpmvStoreYhost.hpp:27-55, and the krnl_dStoreY kernel,
  * dSpmv/hw/include/impl/dStoreY.hpp:36-65).  Reads numNodes transY frames
