@@ -19,6 +19,8 @@
 // cgVector.hpp:101-114) and the instruction slot 0 (cgVector.hpp:149-159).
 // Reductions are fixed-order (per-CTA tree, then the last CTA sums the CTA
 // partials in index order), so a solve is bitwise reproducible.
+#include <algorithm>
+
 #include "xjpcg_device.cuh"
 #include "xjpcg_internal.hpp"
 
@@ -74,6 +76,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_init_kernel(int n, int n4, con
         s->tols = fin[0] * s->tol * s->tol;
         s->k = 0;
         s->done = 0;
+        s->counters[3] = 0u;  // the fused kernel's grid barrier
         s->status &= ~(kStatusBreakdown | kStatusWaitTimeout);
         s->vecSize = (uint32_t)n4;
         if (s->records && s->recCap > 0) {
@@ -200,6 +203,118 @@ __global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double*
     }
 }
 
+// The update and the p update fused into one cooperative launch.
+//   phase A  r' = r - alpha Ap, z = J r', x' = x + alpha p, and the CTA's
+//            partial r'.r' and r'.z; r' and x' are written with streaming
+//            stores, z over the spent Ap with an L2 evict-last policy, and p
+//            is read with that policy, so that both are still in L2 after
+//  barrier  a bounded grid barrier (all CTAs are resident: cooperative
+//            launch), after which every CTA sums all CTAs' partials in the
+//            same fixed order, so each holds the same r.r, r.z and beta;
+//   phase B  p' = z + beta p over the same elements (same thread, same
+//            elements as phase A, so no other CTA's writes are read), with p'
+//            stored evict-last for the next SpMV's gathers; CTA 0 writes the
+//            record, applies the stop rule and sets the loop's condition.
+// An iteration then streams 64 n bytes of vectors from HBM (phase A reads
+// r, Ap, J, x, p and writes r', x'; phase B writes p') instead of 80 n, with
+// one launch and no last-CTA reduction tail.  Same arithmetic per element as
+// cg_update_kernel + cg_pupdate_kernel; only the order of the r.r / r.z sums
+// differs (per CTA, then over CTAs), and it is fixed.
+constexpr uint64_t kBarrierBudgetNs = 2000000000ull;  // 2 s
+
+__global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* __restrict__ x,
+                                                               double* __restrict__ r, double* __restrict__ p,
+                                                               double* __restrict__ Apz,
+                                                               const double* __restrict__ J, CgState* state,
+                                                               double* partials) {
+    // Uniform in every CTA: done only changes after the barrier below.
+    if (*(volatile uint32_t*)&state->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            state->xSkip = 1u;
+            if (state->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)state->condHandle, 0u);
+        }
+        return;
+    }
+    const double alpha = state->alpha;
+    const double rzOld = state->rz;  // CTA 0 overwrites it after the barrier
+    const uint32_t k0 = state->k;
+    const uint64_t keep = l2_policy_evict_last();
+    const int n2 = n4 >> 1;
+    double2* r2 = reinterpret_cast<double2*>(r);
+    double2* x2 = reinterpret_cast<double2*>(x);
+    double2* p2 = reinterpret_cast<double2*>(p);
+    double2* z2 = reinterpret_cast<double2*>(Apz);
+    const double2* j2 = reinterpret_cast<const double2*>(J);
+    const int stride = gridDim.x * blockDim.x;
+    double rr = 0.0, rz = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
+        double2 rv = __ldcs(&r2[i]);
+        const double2 av = __ldcs(&z2[i]), jv = __ldcs(&j2[i]);
+        double2 xv = __ldcs(&x2[i]);
+        const double2 pv = ld2_policy(&p2[i], keep);
+        rv.x = fma(-alpha, av.x, rv.x);
+        rv.y = fma(-alpha, av.y, rv.y);
+        const double2 zv = make_double2(rv.x * jv.x, rv.y * jv.y);
+        xv.x = fma(alpha, pv.x, xv.x);
+        xv.y = fma(alpha, pv.y, xv.y);
+        rr = fma(rv.x, rv.x, rr);
+        rr = fma(rv.y, rv.y, rr);
+        rz = fma(rv.x, zv.x, rz);
+        rz = fma(rv.y, zv.y, rz);
+        __stcs(&r2[i], rv);
+        __stcs(&x2[i], xv);
+        st2_policy(&z2[i], zv, keep);
+    }
+    double v[2] = {rr, rz};
+    block_sum<kVecThreads, 2, double>(v);
+    const int nb = gridDim.x;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = v[0];
+        partials[nb + blockIdx.x] = v[1];
+    }
+    if (!grid_barrier_bounded(&state->counters[3], &state->counters[5], kBarrierBudgetNs)) {
+        if (threadIdx.x == 0) {
+            atomicOr(&state->status, kStatusWaitTimeout);
+            state->done = 1u;
+            if (state->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)state->condHandle, 0u);
+        }
+        return;
+    }
+    // Every CTA forms the totals from all partials, in one fixed order.
+    double s[2] = {0.0, 0.0};
+    for (int b = threadIdx.x; b < nb; b += kVecThreads) {
+        s[0] += __ldcg(&partials[b]);
+        s[1] += __ldcg(&partials[nb + b]);
+    }
+    block_allsum<kVecThreads, 2, double>(s);
+    const double rrN = s[0], rzN = s[1];
+    const double beta = rzN / rzOld;
+    bool cont = !(rrN < state->tols) && (k0 + 1u < state->maxIterP1);
+    if (!isfinite(alpha) || !isfinite(beta) || !isfinite(rrN)) cont = false;
+    if (cont) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
+            const double2 zv = ld2_policy(&z2[i], keep);
+            double2 pv = ld2_policy(&p2[i], keep);
+            pv.x = fma(beta, pv.x, zv.x);
+            pv.y = fma(beta, pv.y, zv.y);
+            st2_policy(&p2[i], pv, keep);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        CgState* st = state;
+        st->rr = rrN;
+        st->rz = rzN;
+        st->beta = beta;
+        write_record(st, k0, rrN, rzN, alpha, beta);
+        if (!isfinite(alpha) || !isfinite(beta) || !isfinite(rrN)) st->status |= kStatusBreakdown;
+        if (st->status & kStatusWaitTimeout) cont = false;
+        st->k = k0 + 1u;
+        st->xSkip = 0u;
+        st->done = cont ? 0u : 1u;
+        if (st->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)st->condHandle, cont ? 1u : 0u);
+    }
+}
+
 // Diagnostic of the bounded wait that every mbarrier wait in the library
 // uses (mbar_wait_bounded).  One warp initialises an mbarrier that expects
 // one arrival and never arrives, so the wait cannot complete: it must give up
@@ -296,6 +411,33 @@ cudaError_t cg_update_launch(int grid, cudaStream_t st, int n4, double* r, doubl
                              CgState* state, double* partials) {
     cg_update_kernel<<<grid, kVecThreads, 0, st>>>(n4, r, Ap, J, state, partials);
     return cudaGetLastError();
+}
+
+// One CTA per resident slot: the cooperative launch needs them all at once.
+int fused_grid(int n4, int numSms) {
+    int perSm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, cg_fused_kernel, kVecThreads, 0) != cudaSuccess ||
+        perSm < 1) {
+        cudaGetLastError();
+        perSm = 1;
+    }
+    const int need = std::max(1, (n4 / 2 + kVecThreads - 1) / kVecThreads);
+    return std::min(need, numSms * perSm);
+}
+
+cudaError_t cg_fused_launch(int grid, cudaStream_t st, int n4, double* x, double* r, double* p, double* Apz,
+                            const double* J, CgState* state, double* partials) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kVecThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, cg_fused_kernel, n4, x, r, p, Apz, J, state, partials);
 }
 
 cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* z,

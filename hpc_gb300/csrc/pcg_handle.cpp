@@ -149,6 +149,7 @@ void PcgHandle::init(int device) {
     check(cudaMemsetAsync(m_state32.p, 0, sizeof(CgState), m_stream), "memset");
     check(cudaStreamSynchronize(m_stream), "sync");
     m_useGraph = envInt("XJPCG_HOST_LOOP", 0) == 0;
+    m_fusedUpdate = envInt("XJPCG_FUSED_UPDATE", 1) != 0;
     m_forcedLanes = envInt("XJPCG_SPMV_LANES", 0);
     m_forcedCfg = envInt("XJPCG_SPMV_CFG", -1);
     m_faultAlloc = envIs("XJPCG_FAULT", "alloc");
@@ -976,15 +977,29 @@ void PcgHandle::buildGraph() {
     check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part, kSpmvCgDot,
                               &st->done),
           "SpMV kernel");
-    check(cg_update_launch(update_grid(n4, m_numSms), m_stream, n4, m_r.as<double>(), m_Ap.as<double>(),
-                                       m_J.as<double>(), st, part),
-          "update kernel");
-    check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_Ap.as<double>(), st),
-          "p kernel");
+    iterationTail(n4, st, part);
     check(cudaStreamEndCapture(m_stream, &body), "capture body end");
     check(cudaGraphInstantiate(&m_exec, g, 0), "graph instantiate");
     cudaGraphDestroy(g);
     m_execGen = m_generation;
+}
+
+// The vector part of an fp64 iteration after the SpMV: the fused cooperative
+// kernel (update and p update in one launch), or the two separate kernels
+// when XJPCG_FUSED_UPDATE=0.
+void PcgHandle::iterationTail(int n4, CgState* st, double* part) {
+    if (m_fusedUpdate) {
+        check(cg_fused_launch(fused_grid(n4, m_numSms), m_stream, n4, m_x.as<double>(), m_r.as<double>(),
+                              m_p.as<double>(), m_Ap.as<double>(), m_J.as<double>(), st, part),
+              "fused update kernel");
+        return;
+    }
+    check(cg_update_launch(update_grid(n4, m_numSms), m_stream, n4, m_r.as<double>(), m_Ap.as<double>(),
+                           m_J.as<double>(), st, part),
+          "update kernel");
+    check(cg_pupdate_launch(vec_grid(n4, m_numSms), m_stream, n4, m_x.as<double>(), m_p.as<double>(),
+                            m_Ap.as<double>(), st),
+          "p kernel");
 }
 
 Results PcgHandle::run(uint32_t maxIter, double tol) {
@@ -1028,11 +1043,7 @@ Results PcgHandle::run(uint32_t maxIter, double tol) {
                 check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part,
                                           kSpmvCgDot, &st->done),
                       "SpMV kernel");
-                check(cg_update_launch(update_grid(n4, m_numSms), m_stream, n4, m_r.as<double>(), m_Ap.as<double>(),
-                                       m_J.as<double>(), st, part),
-                      "update kernel");
-                check(cg_pupdate_launch(vg, m_stream, n4, m_x.as<double>(), m_p.as<double>(), m_Ap.as<double>(), st),
-                      "p kernel");
+                iterationTail(n4, st, part);
             }
             ran += 16;
             uint32_t done = 0;

@@ -206,6 +206,7 @@ class PcgHandle {
                        int mode, const uint32_t* done);
     void ensureVectors(uint32_t n);
     void buildGraph();
+    void iterationTail(int n4, CgState* st, double* part);
     void buildMixedGraph();
     Results readResults(uint32_t maxIter);
 
@@ -317,6 +318,7 @@ class PcgHandle {
     uint64_t m_mixedGen = 0;
     cudaGraphConditionalHandle m_condOuter = 0, m_condInner = 0;
     bool m_useGraph = true;
+    bool m_fusedUpdate = true;  // XJPCG_FUSED_UPDATE
     bool m_faultAlloc = false, m_faultLaunch = false, m_initDone = false;  // XJPCG_FAULT hooks
     size_t m_guardBytes = 0;                                   // XJPCG_GUARD_BYTES
     std::vector<std::pair<DevBuf*, std::string>> m_guarded;    // buffers allocated with guards

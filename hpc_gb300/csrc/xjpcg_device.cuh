@@ -175,6 +175,58 @@ __device__ __forceinline__ uint64_t l2_policy_evict_first() {
     return pol;
 }
 
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// 16-byte global load / store with an L2 cache policy from createpolicy.
+__device__ __forceinline__ double2 ld2_policy(const double2* p, uint64_t pol) {
+    double2 v;
+    asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ void st2_policy(double2* p, double2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y), "l"(pol)
+                 : "memory");
+}
+
+// Grid-wide barrier for a cooperative launch (every CTA resident), bounded:
+// thread 0 of each CTA arrives on *count; the last one to arrive resets it
+// and advances *gen, which the others wait for.  A wait that outlasts
+// budgetNs of %globaltimer gives up and returns false (the caller records
+// kStatusWaitTimeout); every CTA's writes before the barrier are visible to
+// every CTA after it.  count must be 0 before the launch.
+__device__ __forceinline__ bool grid_barrier_bounded(uint32_t* count, uint32_t* gen, uint64_t budgetNs) {
+    __shared__ bool ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = true;
+        const uint32_t g = *(volatile uint32_t*)gen;
+        __threadfence();
+        const uint32_t arrived = atomicAdd(count, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            *(volatile uint32_t*)count = 0u;
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            const uint64_t t0 = globaltimer_ns();
+            while (*(volatile uint32_t*)gen == g) {
+                if (globaltimer_ns() - t0 > budgetNs) {
+                    ok = false;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok;
+}
+
 // 1-D bulk copy global -> shared, completing on the mbarrier's transaction
 // count.  dst, src and bytes must all be multiples of 16.
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint64_t pol) {

@@ -143,6 +143,11 @@ cudaError_t residual_finish_launch(cudaStream_t st, int n, const VT* b, VT* y, d
 // ---- CG vector kernels (cg_kernels.cu) ----
 int vec_grid(int n4, int numSms);
 int update_grid(int n4, int numSms);
+// update + p update in one cooperative launch (cg_kernels.cu); grid from
+// fused_grid (every CTA resident); partials hold 2 * grid doubles.
+int fused_grid(int n4, int numSms);
+cudaError_t cg_fused_launch(int grid, cudaStream_t st, int n4, double* x, double* r, double* p, double* Apz,
+                            const double* J, CgState* state, double* partials);
 cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x,
                            double* r, double* p, double* J, double* Ap, CgState* state, double* partials);
 // update: r -= alpha Ap, then z = J r is written over Ap; p update reads it

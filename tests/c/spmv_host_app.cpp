@@ -13,8 +13,11 @@
 // dSpmvComputeHost<16> on the same matrix and send their rows over a
 // NetStream, card 0 at memory word 0 and card 1 right after card 0's rows
 // (rounded up to whole 64-byte words); the store card's dSpmvStoreYhost<16>
-// assembles them.  Both halves must equal part 1's y bit for bit, and the
-// words between them must hold the transY zero fill.
+// assembles them.  Each half must equal its card's y bit for bit (the
+// compute -> frame -> store round trip), the words after each half must hold
+// the transY zero fill, and each card's y must pass the reference test's
+// compare against refVec (each card tunes its own SpMV, so the cards' sums
+// may differ from part 1's in the last bits).
 //
 // Usage: spmv_host_app <sig_dir> <vec_dir> [device id]; prints
 // "INFO: Test pass!" and exits 0 when every check holds.
@@ -146,8 +149,15 @@ int main(int argc, char** argv) {
         }
         for (int c = 0; c < 2; ++c) {
             const double* part = mem.data() + (c == 0 ? 0 : 4 * (size_t)start1);
-            if (std::memcmp(part, y.data(), yRows * sizeof(double)) != 0) {
-                std::cout << "ERROR: dSpmv: card " << c << "'s rows differ from SpmvHost's y" << std::endl;
+            const std::vector<double>& yc = compute[c].y();
+            if (yc.size() != yRows || std::memcmp(part, yc.data(), yRows * sizeof(double)) != 0) {
+                std::cout << "ERROR: dSpmv: the stored rows of card " << c << " differ from its y" << std::endl;
+                return EXIT_FAILURE;
+            }
+            int cerrs = 0;
+            for (unsigned int i = 0; i < yRows; ++i) cerrs += isClose(yc[i], ref[i]) ? 0 : 1;
+            if (cerrs != 0) {
+                std::cout << "ERROR: dSpmv: card " << c << ": " << cerrs << " entries mismatch refVec" << std::endl;
                 return EXIT_FAILURE;
             }
             for (size_t i = yRows; i < 8 * (size_t)words0; ++i)
