@@ -209,12 +209,13 @@ __global__ void __launch_bounds__(kVecThreads) cg_pupdate_kernel(int n4, double*
 //            stores, z over the spent Ap with an L2 evict-last policy, and p
 //            is read with that policy, so that both are still in L2 after
 //  barrier  a bounded grid barrier (all CTAs are resident: cooperative
-//            launch), after which every CTA sums all CTAs' partials in the
-//            same fixed order, so each holds the same r.r, r.z and beta;
+//            launch); the last CTA to arrive adds all CTAs' partials in a
+//            fixed order, forms beta, writes the record, applies the stop
+//            rule and sets the loop's condition, once, and publishes beta
+//            and that decision before releasing the others;
 //   phase B  p' = z + beta p over the same elements (same thread, same
 //            elements as phase A, so no other CTA's writes are read), with p'
-//            stored evict-last for the next SpMV's gathers; CTA 0 writes the
-//            record, applies the stop rule and sets the loop's condition.
+//            stored evict-last for the next SpMV's gathers.
 // An iteration then streams 64 n bytes of vectors from HBM (phase A reads
 // r, Ap, J, x, p and writes r', x'; phase B writes p') instead of 80 n, with
 // one launch and no last-CTA reduction tail.  Same arithmetic per element as
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
         return;
     }
     const double alpha = state->alpha;
-    const double rzOld = state->rz;  // CTA 0 overwrites it after the barrier
+    const double rzOld = state->rz;  // the last CTA at the barrier overwrites it
     const uint32_t k0 = state->k;
     const uint64_t keep = l2_policy_evict_last();
     const int n2 = n4 >> 1;
@@ -267,12 +268,32 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
     }
     double v[2] = {rr, rz};
     block_sum<kVecThreads, 2, double>(v);
-    const int nb = gridDim.x;
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x] = v[0];
-        partials[nb + blockIdx.x] = v[1];
-    }
-    if (!grid_barrier_bounded(&state->counters[3], &state->counters[5], kBarrierBudgetNs)) {
+    // The last CTA at the barrier has the grid's r.r and r.z: it forms beta,
+    // writes the record, applies the stop rule (control.hpp:83), sets the
+    // loop's condition and publishes beta and the decision for the others.
+    auto finish = [state, alpha, rzOld, k0](const double (&tot)[2]) {
+        CgState* st = state;
+        const double rrN = tot[0], rzN = tot[1];
+        const double beta = rzN / rzOld;
+        bool cont = !(rrN < st->tols) && (k0 + 1u < st->maxIterP1);
+        if (!isfinite(alpha) || !isfinite(beta) || !isfinite(rrN)) {
+            st->status |= kStatusBreakdown;
+            cont = false;
+        }
+        if (st->status & kStatusWaitTimeout) cont = false;
+        st->rr = rrN;
+        st->rz = rzN;
+        st->beta = beta;
+        write_record(st, k0, rrN, rzN, alpha, beta);
+        st->k = k0 + 1u;
+        st->xSkip = 0u;
+        st->done = cont ? 0u : 1u;
+        st->fusedBeta = beta;
+        st->fusedCont = cont ? 1u : 0u;
+        if (st->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)st->condHandle, cont ? 1u : 0u);
+    };
+    if (!grid_sum_barrier<kVecThreads, 2>(v, partials, &state->counters[3], &state->counters[5], finish,
+                                          kBarrierBudgetNs)) {
         if (threadIdx.x == 0) {
             atomicOr(&state->status, kStatusWaitTimeout);
             state->done = 1u;
@@ -280,18 +301,8 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
         }
         return;
     }
-    // Every CTA forms the totals from all partials, in one fixed order.
-    double s[2] = {0.0, 0.0};
-    for (int b = threadIdx.x; b < nb; b += kVecThreads) {
-        s[0] += __ldcg(&partials[b]);
-        s[1] += __ldcg(&partials[nb + b]);
-    }
-    block_allsum<kVecThreads, 2, double>(s);
-    const double rrN = s[0], rzN = s[1];
-    const double beta = rzN / rzOld;
-    bool cont = !(rrN < state->tols) && (k0 + 1u < state->maxIterP1);
-    if (!isfinite(alpha) || !isfinite(beta) || !isfinite(rrN)) cont = false;
-    if (cont) {
+    const double beta = __ldcg(&state->fusedBeta);
+    if (__ldcg(&state->fusedCont)) {
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
             const double2 zv = ld2_policy(&z2[i], keep);
             double2 pv = ld2_policy(&p2[i], keep);
@@ -299,19 +310,6 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
             pv.y = fma(beta, pv.y, zv.y);
             st2_policy(&p2[i], pv, keep);
         }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        CgState* st = state;
-        st->rr = rrN;
-        st->rz = rzN;
-        st->beta = beta;
-        write_record(st, k0, rrN, rzN, alpha, beta);
-        if (!isfinite(alpha) || !isfinite(beta) || !isfinite(rrN)) st->status |= kStatusBreakdown;
-        if (st->status & kStatusWaitTimeout) cont = false;
-        st->k = k0 + 1u;
-        st->xSkip = 0u;
-        st->done = cont ? 0u : 1u;
-        if (st->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)st->condHandle, cont ? 1u : 0u);
     }
 }
 

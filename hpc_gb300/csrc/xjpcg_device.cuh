@@ -193,33 +193,54 @@ __device__ __forceinline__ void st2_policy(double2* p, double2 v, uint64_t pol) 
                  : "memory");
 }
 
-// Grid-wide barrier for a cooperative launch (every CTA resident), bounded:
-// thread 0 of each CTA arrives on *count; the last one to arrive resets it
-// and advances *gen, which the others wait for.  A wait that outlasts
-// budgetNs of %globaltimer gives up and returns false (the caller records
-// kStatusWaitTimeout); every CTA's writes before the barrier are visible to
-// every CTA after it.  count must be 0 before the launch.
-__device__ __forceinline__ bool grid_barrier_bounded(uint32_t* count, uint32_t* gen, uint64_t budgetNs) {
-    __shared__ bool ok;
-    __syncthreads();
+// Grid-wide sum of NV doubles fused with a grid barrier, for a cooperative
+// launch (every CTA resident).  Each CTA passes its block total (thread 0);
+// the last CTA to arrive adds all CTAs' totals in index order (its threads
+// take t, t + NT, ... then block_sum's fixed order) and calls fin(sums) in
+// its thread 0 -- the one place where the grid's totals exist, so whatever
+// follows from them is computed once -- then releases the others.  Writes
+// made by fin are visible to every CTA after the barrier.  A wait longer
+// than budgetNs of %globaltimer gives up and returns false.  count must be 0
+// before the launch; partials holds NV * gridDim.x doubles.
+template <int NT, int NV, typename Fin>
+__device__ __forceinline__ bool grid_sum_barrier(const double (&blockTotal)[NV], double* partials, uint32_t* count,
+                                                 uint32_t* gen, Fin fin, uint64_t budgetNs) {
+    __shared__ bool amLast, ok;
+    __shared__ uint32_t genSeen;
+    const int nb = gridDim.x;
     if (threadIdx.x == 0) {
         ok = true;
-        const uint32_t g = *(volatile uint32_t*)gen;
+        genSeen = *(volatile uint32_t*)gen;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) partials[i * nb + blockIdx.x] = blockTotal[i];
         __threadfence();
-        const uint32_t arrived = atomicAdd(count, 1u) + 1u;
-        if (arrived == gridDim.x) {
+        amLast = atomicAdd(count, 1u) == (uint32_t)nb - 1u;
+    }
+    __syncthreads();
+    if (amLast) {
+        __threadfence();
+        double s[NV];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double a = 0.0;
+            for (int b = threadIdx.x; b < nb; b += NT) a += __ldcg(&partials[i * nb + b]);
+            s[i] = a;
+        }
+        block_sum<NT, NV, double>(s);
+        if (threadIdx.x == 0) {
+            fin(s);
             *(volatile uint32_t*)count = 0u;
             __threadfence();
             atomicAdd(gen, 1u);
-        } else {
-            const uint64_t t0 = globaltimer_ns();
-            while (*(volatile uint32_t*)gen == g) {
-                if (globaltimer_ns() - t0 > budgetNs) {
-                    ok = false;
-                    break;
-                }
-                __nanosleep(64);
+        }
+    } else if (threadIdx.x == 0) {
+        const uint64_t t0 = globaltimer_ns();
+        while (*(volatile uint32_t*)gen == genSeen) {
+            if (globaltimer_ns() - t0 > budgetNs) {
+                ok = false;
+                break;
             }
+            __nanosleep(32);
         }
         __threadfence();
     }

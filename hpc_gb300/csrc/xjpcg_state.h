@@ -49,6 +49,8 @@ struct alignas(16) CgState {
     uint32_t skipRefresh;          // mixed precision: 1 = the refresh kernels of this iteration return at once
     uint32_t xSkip;                // fp64: 1 = the update kernel found the loop done (no x update due)
     uint32_t pupdateDue;           // reference-order loop: 1 = this iteration's p update is due
+    uint32_t fusedCont;            // fused update: 1 = the loop goes on (the p update is due)
+    double fusedBeta;              // fused update: beta, published at its grid barrier
 };
 
 }  // namespace xjpcg
