@@ -455,6 +455,35 @@ def test_host_loop_matches_graph_loop(gpu_lib):
     assert a.iters == b.iters and np.array_equal(a.x, b.x)
 
 
+def test_fused_and_separate_vector_kernels_agree(gpu_lib):
+    """The fp64 iteration's vector work runs as one cooperative launch (the
+    default) or as the update and p-update kernels (XJPCG_FUSED_UPDATE=0).
+    Both meet the oracle's bar, in the graph loop and the host loop; the
+    per-element arithmetic is the same, only the order of the r.r / r.z sums
+    differs."""
+    s = W.diffusion27(24, seed=12)
+    ref = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
+    os.environ["XJPCG_SPMV_LANES"] = "-1"
+    out = {}
+    try:
+        for fused in ("1", "0"):
+            for host in ("0", "1"):
+                os.environ["XJPCG_FUSED_UPDATE"] = fused
+                os.environ["XJPCG_HOST_LOOP"] = host
+                with X.JPCG() as h:
+                    r = h.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
+                assert r.status == X.SUCCESS, r.message
+                assert abs(r.iters - ref["iters"]) <= max(1, 0.01 * ref["iters"])
+                assert np.linalg.norm(r.x - ref["x"]) / np.linalg.norm(ref["x"]) <= X_TOL
+                out[fused, host] = r
+    finally:
+        for k in ("XJPCG_SPMV_LANES", "XJPCG_FUSED_UPDATE", "XJPCG_HOST_LOOP"):
+            os.environ.pop(k, None)
+    for fused in ("1", "0"):  # graph and host loops launch the same kernels: same bits
+        a, b = out[fused, "0"], out[fused, "1"]
+        assert a.iters == b.iters and np.array_equal(a.x, b.x)
+
+
 @pytest.mark.parametrize("lanes", ["-3", "-2"])
 def test_mixed_host_loop_matches_graph_loop(gpu_lib, lanes):
     # the mixed solver's host-driven loop (used under profilers) runs the
