@@ -640,8 +640,8 @@ def run_gb300(args):
             e2e_step()
             step_s.append(time.perf_counter() - ts)
             m_, i_ = h.metrics(), h.info()
-            step_phases.append([round(m_.m_matProc, 4), round(i_.uploadMs / 1e3, 4), round(i_.tuneMs / 1e3, 4),
-                                round(m_.m_solver, 4)])
+            step_phases.append([round(m_.m_matProc, 4), round(i_.uploadMs / 1e3, 4), round(i_.uploadIdxMs / 1e3, 4),
+                                round(i_.uploadValMs / 1e3, 4), round(i_.tuneMs / 1e3, 4), round(m_.m_solver, 4)])
         torch.cuda.synchronize()
         te = max_over_ranks(time.perf_counter() - t0)
         met, inf_e = h.metrics(), h.info()
@@ -649,7 +649,8 @@ def run_gb300(args):
                "h2d_bytes_per_step": int(4 * nnz + 4 * nnz + 8 * nnz + 8 * n + 8 * n),
                "d2h_bytes_per_step": int(8 * n + 256), "time_to_tol_s": te / args.steps,
                "call": "xJPCG_cooSolver(MODE_DEFAULT), pinned host COO arrays", "step_s": step_s,
-               "step_phases_s": {"columns": ["matProc", "upload", "tuning", "solver"], "steps": step_phases},
+               "step_phases_s": {"columns": ["matProc", "upload", "upload_indices", "upload_values", "tuning",
+                                                 "solver"], "steps": step_phases},
                "last_call_phases_s": {"matProc (H2D, conversion, layouts, tuning)": met.m_matProc,
                                       "of which SpMV tuning": inf_e.tuneMs / 1e3,
                                       "of which H2D of the COO arrays": inf_e.uploadMs / 1e3,

@@ -59,7 +59,8 @@ class GbInfo(C.Structure):
                 ("spmvLayout", C.c_uint32), ("batchThreads", C.c_uint32), ("batchLanes", C.c_uint32),
                 ("batchSmemRows", C.c_uint32), ("batchGrid", C.c_uint32), ("batchMs", C.c_double),
                 ("spmvCfg", C.c_uint32), ("spmvCfg32", C.c_uint32), ("spmvLayout32", C.c_uint32),
-                ("batchSliced", C.c_uint32), ("tuneMs", C.c_double), ("uploadMs", C.c_double)]
+                ("batchSliced", C.c_uint32), ("tuneMs", C.c_double), ("uploadMs", C.c_double),
+                ("uploadIdxMs", C.c_double), ("uploadValMs", C.c_double)]
 
 
 class GbSignature(C.Structure):

@@ -71,6 +71,8 @@ PcgHandle::~PcgHandle() {
     if (m_ev1) cudaEventDestroy(m_ev1);
     if (m_evUp0) cudaEventDestroy(m_evUp0);
     if (m_evUp1) cudaEventDestroy(m_evUp1);
+    if (m_evUpIdx) cudaEventDestroy(m_evUpIdx);
+    if (m_evUpVal) cudaEventDestroy(m_evUpVal);
     if (m_evIdxIn) cudaEventDestroy(m_evIdxIn);
     if (m_upStream) cudaStreamDestroy(m_upStream);
     if (m_stream) cudaStreamDestroy(m_stream);
@@ -139,6 +141,8 @@ void PcgHandle::init(int device) {
     check(cudaEventCreate(&m_ev1), "cudaEventCreate");
     check(cudaEventCreate(&m_evUp0), "cudaEventCreate");
     check(cudaEventCreate(&m_evUp1), "cudaEventCreate");
+    check(cudaEventCreate(&m_evUpIdx), "cudaEventCreate");
+    check(cudaEventCreate(&m_evUpVal), "cudaEventCreate");
     check(cudaEventCreateWithFlags(&m_evIdxIn, cudaEventDisableTiming), "cudaEventCreate");
     check(cudaStreamCreateWithFlags(&m_upStream, cudaStreamNonBlocking), "cudaStreamCreate");
     alloc(m_state, sizeof(CgState), "solver state");
@@ -176,7 +180,9 @@ void PcgHandle::setCooMat(uint32_t n, uint64_t nnz, const uint32_t* row, const u
     check(cudaMemcpyAsync(m_inRow.p, row, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D rows");
     check(cudaMemcpyAsync(m_inCol.p, col, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, m_stream), "H2D cols");
     check(cudaEventRecord(m_evIdxIn, m_stream), "event");
+    check(cudaEventRecord(m_evUpIdx, m_stream), "event");
     check(cudaStreamWaitEvent(m_upStream, m_evIdxIn, 0), "stream wait");
+    check(cudaEventRecord(m_evUpVal, m_upStream), "event");
     check(cudaMemcpyAsync(m_inVal.p, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, m_upStream), "H2D values");
     check(cudaEventRecord(m_evUp1, m_upStream), "event");
     m_uploadTimed = true;
@@ -1978,6 +1984,8 @@ void PcgHandle::fillInfo(XJPCG_GbInfo_t* info) const {
     info->tuneMs = m_lastTuneMs;
     float up = 0.f;
     if (m_uploadTimed && cudaEventElapsedTime(&up, m_evUp0, m_evUp1) == cudaSuccess) info->uploadMs = up;
+    if (m_uploadTimed && cudaEventElapsedTime(&up, m_evUp0, m_evUpIdx) == cudaSuccess) info->uploadIdxMs = up;
+    if (m_uploadTimed && cudaEventElapsedTime(&up, m_evUpVal, m_evUp1) == cudaSuccess) info->uploadValMs = up;
 }
 
 }  // namespace xjpcg

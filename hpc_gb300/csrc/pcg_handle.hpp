@@ -274,6 +274,7 @@ class PcgHandle {
     std::vector<float> m_tuneMs32;
     double m_lastTuneMs = 0.0;  // wall time of the last FP64 tuning
     cudaEvent_t m_evUp0 = nullptr, m_evUp1 = nullptr;  // around the last COO upload
+    cudaEvent_t m_evUpIdx = nullptr, m_evUpVal = nullptr;  // end of the index copies, start of the value copy
     bool m_uploadTimed = false;
 
     // vectors

@@ -47,6 +47,8 @@ typedef struct {
     uint32_t batchSliced;  /* batched solves: 1 when the chosen kernel reads the per-system SELL-32 copy */
     double tuneMs;         /* wall time of the last SpMV tuning (part of m_matProc) */
     double uploadMs;       /* device time of the last COO matrix upload (H2D, part of m_matProc) */
+    double uploadIdxMs;    /* of which the row and column index copies (on the handle's stream) */
+    double uploadValMs;    /* of which the value copy (on the side stream, from its start) */
 } XJPCG_GbInfo_t;
 
 /* Per-system outcome of a batched solve. */
