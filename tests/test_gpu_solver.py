@@ -458,9 +458,9 @@ def test_host_loop_matches_graph_loop(gpu_lib):
 def test_fused_and_separate_vector_kernels_agree(gpu_lib):
     """The fp64 iteration's vector work runs as one cooperative launch (the
     default) or as the update and p-update kernels (XJPCG_FUSED_UPDATE=0).
-    Both meet the oracle's bar, in the graph loop and the host loop; the
-    per-element arithmetic is the same, only the order of the r.r / r.z sums
-    differs."""
+    Both meet the oracle's bar, in the graph loop and the host loop, and the
+    mixed solver beside them too; the per-element arithmetic is the same,
+    only the order of the r.r / r.z sums differs."""
     s = W.diffusion27(24, seed=12)
     ref = oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
     os.environ["XJPCG_SPMV_LANES"] = "-1"
@@ -472,9 +472,13 @@ def test_fused_and_separate_vector_kernels_agree(gpu_lib):
                 os.environ["XJPCG_HOST_LOOP"] = host
                 with X.JPCG() as h:
                     r = h.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10)
+                    m = h.mixed_solve(s.b, s.diag, 20000, 1e-10)  # the mixed loop's FP32 update
                 assert r.status == X.SUCCESS, r.message
                 assert abs(r.iters - ref["iters"]) <= max(1, 0.01 * ref["iters"])
                 assert np.linalg.norm(r.x - ref["x"]) / np.linalg.norm(ref["x"]) <= X_TOL
+                assert m.status == X.SUCCESS, m.message
+                assert oracle.true_relres(s.rowptr, s.col, s.val, s.b, m.x) <= 1.5e-10
+                assert np.linalg.norm(m.x - ref["x"]) / np.linalg.norm(ref["x"]) <= X_TOL
                 out[fused, host] = r
     finally:
         for k in ("XJPCG_SPMV_LANES", "XJPCG_FUSED_UPDATE", "XJPCG_HOST_LOOP"):
