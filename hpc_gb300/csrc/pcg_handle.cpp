@@ -1930,7 +1930,7 @@ int PcgHandle::tuning(float* ms, int* shape, int cap) const {
             shape[4 * c] = 1;
             shape[4 * c + 1] = 2;
             shape[4 * c + 2] = sellpat_config_unroll(c - patCfg0());
-            shape[4 * c + 3] = sellpat_config_tma(c - patCfg0());
+            shape[4 * c + 3] = sellpat_config_tma(c - patCfg0()) ? 1 : (sellpat_config_runs(c - patCfg0()) ? 2 : 0);
         } else if (isSorted(c)) {
             // length-sorted sliced layout: (1, 1, unroll, 32)
             shape[4 * c] = 1;

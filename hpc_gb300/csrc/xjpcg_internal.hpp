@@ -69,6 +69,7 @@ cudaError_t spmv_sell_launch(int cfg, int grid, cudaStream_t st, int n, const in
 int sellpat_num_configs();
 int sellpat_config_unroll(int cfg);
 int sellpat_config_tma(int cfg);  // 1: values prefetched by TMA bulk copies (FP32 only)
+int sellpat_config_runs(int cfg);  // 1: run-aware x gathers (consecutive offsets passed by shuffle)
 // All per-slice arrays hold nslices + 1 ints.  totals = {stored values,
 // general-slice columns, stored patterns}.
 cudaError_t sellpat_plan(cudaStream_t st, int n, const int* rowptr, const int* col, int* sliceOff, int* patLen,

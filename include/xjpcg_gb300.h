@@ -255,8 +255,9 @@ XJPCG_Status_t xJPCG_gbGetInfo(const XJPCG_Handle_t* handle, XJPCG_GbInfo_t* inf
  * 32 for absolute int32 columns, 16 for int16 offsets from the row), the
  * length-sorted sliced ones (1, 1, unroll, 32), the shared-offset sliced
  * ones (1, 2, unroll, 1 when TMA bulk copies prefetch the values, a form
- * that exists in FP32 only, else 0) and the merge-path kernel (0, 256, steps
- * per thread, 0).  At most cap
+ * that exists in FP32 only, 2 when runs of consecutive offsets share one
+ * gather through warp shuffles, else 0) and the merge-path kernel (0, 256,
+ * steps per thread, 0).  At most cap
  * configurations are written. */
 XJPCG_Status_t xJPCG_gbGetSpmvTuning(const XJPCG_Handle_t* handle, float* ms, int32_t* shape, int32_t cap,
                                      int32_t* count);

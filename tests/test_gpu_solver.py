@@ -231,15 +231,25 @@ def test_every_forced_config(handle, zipf_small):
 @pytest.mark.parametrize("nx", [30, 41])
 def test_forced_fp32_config_same_bits(handle, nx):
     # the mixed solver's FP32 SpMV forced to each shared-offset form (unroll
-    # 4 and 8, plain loads or TMA-fed values): none changes the order of a
-    # row's FMAs, so the mixed solves agree bit for bit; the TMA-fed forms are
-    # FP32 only; a configuration index out of range is refused
+    # 4 and 8; plain loads, TMA-fed values, or run-aware gathers that pass
+    # consecutive offsets' x values by shuffle): none changes the values or
+    # the order of a row's FMAs, so the mixed solves agree bit for bit; the
+    # TMA-fed forms are FP32 only; a configuration index out of range is
+    # refused.  The FP64 SpMV's run-aware forms give the plain forms' bits.
     s = W.diffusion27(nx, seed=14)
     handle.csr_solve(s.n, s.rowptr, s.col, s.val, s.diag, s.b, 1, 1e-10)
     shapes = [t[:4] for t in handle.spmv_tuning()]
-    cfgs = [shapes.index((1, 2, u, t)) for t in (0, 1) for u in (4, 8)]
+    cfgs = [shapes.index((1, 2, u, t)) for t in (0, 1, 2) for u in (4, 8)]
     with pytest.raises(X.XJPCGError):
         handle.set_spmv_config(cfgs[2])
+    x = np.random.default_rng(5).standard_normal(s.n)
+    ys = []
+    for c in (cfgs[0], cfgs[1], cfgs[4], cfgs[5]):
+        handle.set_spmv_config(c)
+        ys.append(handle.spmv(x))
+    for y in ys[1:]:
+        assert np.array_equal(y, ys[0])
+    handle.set_spmv_config(-1)
     out = []
     for c in cfgs:
         handle.set_spmv_config32(c)
