@@ -83,6 +83,8 @@ def parse():
     ap.add_argument("--workload", choices=["diffusion27", "zipf"], default="diffusion27",
                     help="matrix of --profile: diffusion27(--nx) or the 2M-row Zipf SPD system")
     ap.add_argument("--reps", type=int, default=4)
+    ap.add_argument("--zipf-n", type=int, default=2_000_000,
+                    help="rows of the Zipf SPD system of --profile --workload zipf")
     return ap.parse_args()
 
 
@@ -229,7 +231,7 @@ def run_profile(args):
         print("adjoint forward=%d adjoint=%d status=%d" % (r.iters, it, st), flush=True)
         h.close()
         return
-    sysm = W.diffusion27(args.nx) if args.workload == "diffusion27" else W.zipf_spd(2_000_000, seed=2)
+    sysm = W.diffusion27(args.nx) if args.workload == "diffusion27" else W.zipf_spd(args.zipf_n, seed=2)
     rows, cols, vals = sysm.coo()
     h = X.JPCG()
     r = h.coo_solve(sysm.n, rows, cols, vals, sysm.diag, sysm.b, 0, 1e-10)
