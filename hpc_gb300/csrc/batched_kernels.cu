@@ -140,6 +140,46 @@ __device__ __forceinline__ void block_allreduce(T (&v)[NV]) {
         block_allsum<NT, NV, T>(v);
 }
 
+// block_allreduce of doubles plus one quotient of a total, q = num /
+// total[QI] (OVER = true) or total[QI] / num (OVER = false), formed by warp 0
+// alone, which holds the totals, and returned in every thread with them.  A
+// double divide costs several FMAs on the FP64 pipe, which issues 2 per clock
+// per SM; with every thread of a 512-thread CTA dividing, alpha and beta alone
+// cost about 10 k FP64 operations per system and iteration, whatever the
+// system's size.  (The mixed kernel keeps per-thread divides: its FP64 pipe is
+// otherwise idle, and the helper's registers made its sliced form spill.)
+template <int NT, int NV, int QI, bool OVER>
+__device__ __forceinline__ double block_allreduce_q(double (&v)[NV], double num) {
+    // the narrow form of block_allsum: warp 0 adds every thread's value
+    __shared__ double part[NV][NT];
+    __shared__ double tot[NV];
+    __shared__ double qS;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) part[i][threadIdx.x] = v[i];
+    __syncthreads();
+    if (wid == 0) {
+        double t[NV];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = part[i][lane];
+#pragma unroll 8
+            for (int w = 1; w < NT / 32; ++w) s += part[i][w * 32 + lane];
+            t[i] = warp_sum(s);  // every lane of warp 0 holds the total
+            if (lane == 0) tot[i] = t[i];
+        }
+        // warp 0 divides (32 divides per CTA instead of NT, no divergence)
+        const double q = OVER ? num / t[QI] : t[QI] / num;
+        if (lane == 0) qS = q;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = tot[i];
+    const double q = qS;
+    __syncthreads();  // the next call writes part, tot and qS again
+    return q;
+}
+
 // CG on one system: A d = rhs, d0 = 0, Jacobi preconditioner J.  On entry r
 // holds rhs; on exit d holds the solution increment.  VT is the precision of
 // the vectors and matrix values; reductions leave the CTA in double.
@@ -205,8 +245,7 @@ __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const
             }
         }
         double v1[1] = {(double)pAp};
-        block_allreduce<NT, 1, double>(v1);
-        const double alphaD = rz / v1[0];
+        const double alphaD = block_allreduce_q<NT, 1, 0, true>(v1, rz);  // rz / p.Ap
         const VT alpha = (VT)alphaD;
         AccT rrP = 0, rzP = 0;
         for (int i = tid; i < n; i += NT) {
@@ -220,8 +259,7 @@ __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const
             rzP = fma((AccT)ri, (AccT)zi, rzP);
         }
         double w[2] = {(double)rrP, (double)rzP};
-        block_allreduce<NT, 2, double>(w);
-        const double beta = w[1] / rz;
+        const double beta = block_allreduce_q<NT, 2, 1, false>(w, rz);  // r.z / rz
         rz = w[1];
         rrLast = w[0];
         ++k;
