@@ -6,8 +6,9 @@ record (r.r, r.z, alpha, beta) bit for bit, and x bit for bit.  The matrix is
 the reference partitioner's layout of the system, as this library exports it
 (byte-identical to the reference's own files, tests/test_gpu_signature_export.py)
 and loads it back.  Cases: the reference example's tridiagonal system
-(pcg/sw/examples/c/example.c, n = 65536, maxIter 100, tol 1e-16) and a
-7-point 12^3 system."""
+(pcg/sw/examples/c/example.c, n = 65536, maxIter 100, tol 1e-16), a 7-point
+12^3 system, and the 7-point 32^3 system of the first benchmark configuration
+(142 iterations)."""
 import numpy as np
 import pytest
 
@@ -36,6 +37,10 @@ def _cases():
     s = W.poisson7(12, seed=9)
     rows, cols, vals = s.coo()
     yield "poisson7_12", s.n, rows, cols, vals, s.diag, s.b, 2000, 1e-10
+    # the contract's first configuration: 7-point 32^3, shift 1e-3, b from seed 0
+    s = W.poisson7(32, seed=0)
+    rows, cols, vals = s.coo()
+    yield "poisson7_32", s.n, rows, cols, vals, s.diag, s.b, 2000, 1e-10
 
 
 @pytest.mark.parametrize("case", list(_cases()), ids=lambda c: c[0])
