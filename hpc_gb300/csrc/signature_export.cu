@@ -294,25 +294,44 @@ __global__ void sig_emit_kernel(int S, const int* __restrict__ segLo, const int*
     }
 }
 
-// One thread per partition: the 16 channel cuts, the chunks' extents, the
-// partition's parParam record and the chunks' byte sizes.
+__device__ __forceinline__ int warp_min_i32(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_max_i32(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// One warp per partition: the 16 channel cuts, the chunks' extents, the
+// partition's parParam record and the chunks' byte sizes.  Every lane places
+// the cuts the same way (binary searches over the partition's segments, so
+// control flow stays warp-uniform); the column-group extents of the partition
+// and of each chunk are warp-strided min / max reductions over its segments;
+// lane 0 writes.
 __global__ void sig_chan_kernel(int P, const int* __restrict__ ppad, const int* __restrict__ segFirst,
                                 const int* __restrict__ segOff, const int* __restrict__ segLen,
                                 const int* __restrict__ segRow, const int* __restrict__ segMinG,
                                 const int* __restrict__ segMaxG, int* __restrict__ chStart, int* __restrict__ chLen,
                                 int* __restrict__ chMinG, int* __restrict__ chEndRow,
                                 long long* __restrict__ chBytes, unsigned char* __restrict__ parParam) {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < P; p += warpsPerGrid) {
         const int base = ppad[p], Np = ppad[p + 1] - base;
         const int s0 = segFirst[p], s1 = segFirst[p + 1];
         const int per = Np / kCh;
         uint32_t w[64];
         for (int k = 0; k < 64; ++k) w[k] = 0u;
         int pMinG = 0x7fffffff, pMaxG = -1;
-        for (int s = s0; s < s1; ++s) {
+        for (int s = s0 + lane; s < s1; s += 32) {
             pMinG = min(pMinG, segMinG[s]);
             pMaxG = max(pMaxG, segMaxG[s]);
         }
+        pMinG = warp_min_i32(pMinG);
+        pMaxG = warp_max_i32(pMaxG);
         int start = 0, sa = s0;
         uint16_t cbase[kCh], ccols[kCh];
         for (int c = 0; c < kCh; ++c) {
@@ -330,25 +349,39 @@ __global__ void sig_chan_kernel(int P, const int* __restrict__ ppad, const int* 
                 if (segOff[lo] - base != e) e = segOff[lo] - base + segLen[lo];
             }
             const int len = e - start;
-            int gMin = 0, gMax = -1, endRow = 0;
-            int sb = sa;
-            if (len > 0) {
-                gMin = 0x7fffffff;
-                while (sb < s1 && segOff[sb] - base < e) {
-                    gMin = min(gMin, segMinG[sb]);
-                    gMax = max(gMax, segMaxG[sb]);
-                    ++sb;
-                }
-                endRow = segRow[sb - 1] + 1;
+            // sb: the first segment at or after the cut (segment offsets ascend)
+            int sb = sa, hiS = s1;
+            while (sb < hiS) {
+                const int mid = (sb + hiS) >> 1;
+                if (segOff[mid] - base < e)
+                    sb = mid + 1;
+                else
+                    hiS = mid;
             }
-            const int idx = p * kCh + c;
-            chStart[idx] = start;
-            chLen[idx] = len;
-            chMinG[idx] = gMin;
-            chEndRow[idx] = endRow;
-            const long long words = (len + kRowWordSlots - 1) / kRowWordSlots + (len + kColWordSlots - 1) / kColWordSlots +
-                                    len / kPar;
-            chBytes[(size_t)c * P + p] = 32ll * words;
+            int gMin = 0x7fffffff, gMax = -1;
+            for (int s = sa + lane; s < sb; s += 32) {
+                gMin = min(gMin, segMinG[s]);
+                gMax = max(gMax, segMaxG[s]);
+            }
+            gMin = warp_min_i32(gMin);
+            gMax = warp_max_i32(gMax);
+            int endRow = 0;
+            if (len > 0) {
+                endRow = segRow[sb - 1] + 1;
+            } else {
+                gMin = 0;
+                gMax = -1;
+            }
+            if (lane == 0) {
+                const int idx = p * kCh + c;
+                chStart[idx] = start;
+                chLen[idx] = len;
+                chMinG[idx] = gMin;
+                chEndRow[idx] = endRow;
+                const long long words = (len + kRowWordSlots - 1) / kRowWordSlots +
+                                        (len + kColWordSlots - 1) / kColWordSlots + len / kPar;
+                chBytes[(size_t)c * P + p] = 32ll * words;
+            }
             w[c] = len > 0 ? (uint32_t)(kPar * (gMax - gMin + 1)) : 0u;  // chCols
             w[16 + c] = (uint32_t)len;                                  // chNnzs
             cbase[c] = (uint16_t)((len > 0 ? gMin : 0) - pMinG);         // chBaseAddr
@@ -356,6 +389,7 @@ __global__ void sig_chan_kernel(int P, const int* __restrict__ ppad, const int* 
             start = e;
             sa = sb;
         }
+        if (lane != 0) continue;
         w[32] = (uint32_t)pMinG;                                 // base column group
         w[33] = (uint32_t)(pMaxG - pMinG + 1);                   // column blocks
         w[34] = (uint32_t)(segRow[s1 - 1] - segRow[s0] + 1);     // rows
@@ -699,7 +733,7 @@ void SigExport::build(cudaStream_t st, uint32_t n, uint64_t nnz64, const int* ro
         uint32_t phdr[8] = {(uint32_t)P, 0, 0, 0, 0, 0, 0, 0};
         SIG_CHECK(cudaMemcpyAsync(bPar.p, phdr, sizeof(phdr), cudaMemcpyHostToDevice, st), "H2D");
     }
-    sig_chan_kernel<<<grid_of(P, 64), 64, 0, st>>>(P, bPpad.as<int>(), bSegBase.as<int>(), bSegOff.as<int>(),
+    sig_chan_kernel<<<grid_of((int64_t)P * 32, 256), 256, 0, st>>>(P, bPpad.as<int>(), bSegBase.as<int>(), bSegOff.as<int>(),
                                                     bSegLen.as<int>(), bSegRow.as<int>(), bSegMinG.as<int>(),
                                                     bSegMaxG.as<int>(), bChStart.as<int>(), bChLen.as<int>(),
                                                     bChMinG.as<int>(), bChEndRow.as<int>(),
