@@ -142,7 +142,10 @@ __device__ __forceinline__ void block_allreduce(T (&v)[NV]) {
 
 // block_allreduce of doubles plus one quotient of a total, q = num /
 // total[QI] (OVER = true) or total[QI] / num (OVER = false), formed by warp 0
-// alone, which holds the totals, and returned in every thread with them.  A
+// alone, which holds the totals, and returned in every thread with them.
+// It ends without a barrier: the caller separates two calls of the same
+// instantiation by at least one __syncthreads (cg_core has three between
+// them), so that no thread still reads tot or qS when warp 0 rewrites them.  A
 // double divide costs several FMAs on the FP64 pipe, which issues 2 per clock
 // per SM; with every thread of a 512-thread CTA dividing, alpha and beta alone
 // cost about 10 k FP64 operations per system and iteration, whatever the
@@ -175,9 +178,7 @@ __device__ __forceinline__ double block_allreduce_q(double (&v)[NV], double num)
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = tot[i];
-    const double q = qS;
-    __syncthreads();  // the next call writes part, tot and qS again
-    return q;
+    return qS;
 }
 
 // CG on one system: A d = rhs, d0 = 0, Jacobi preconditioner J.  On entry r
