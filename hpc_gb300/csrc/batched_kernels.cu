@@ -96,13 +96,91 @@ __device__ __forceinline__ AccT slice_dot(const int* __restrict__ sliceOff, int 
     return acc;
 }
 
+// Two slices of one warp at once (j0 and j1), for twice the loads in flight:
+// their batches of 4 columns are interleaved while both slices have one, then
+// each slice finishes alone.  Each slice's FMAs run in its column order, as in
+// slice_dot, so both sums are slice_dot's bit for bit.
+template <typename VT, typename AccT>
+__device__ __forceinline__ void slice_dot2(const int* __restrict__ sliceOff, int j0, int j1,
+                                           const VT* __restrict__ sval, const uint16_t* __restrict__ scol,
+                                           const VT* P, int lane32, AccT& acc0, AccT& acc1) {
+    const int off0 = sliceOff[j0], w0 = (sliceOff[j0 + 1] - off0) >> 5;
+    const int off1 = sliceOff[j1], w1 = (sliceOff[j1 + 1] - off1) >> 5;
+    const VT* vp0 = sval + off0 + lane32;
+    const VT* vp1 = sval + off1 + lane32;
+    const uint16_t* cp0 = scol + off0 + lane32;
+    const uint16_t* cp1 = scol + off1 + lane32;
+    AccT a0 = AccT(0), a1 = AccT(0);
+    const int wm = w0 < w1 ? w0 : w1;
+    int k = 0;
+    for (; k + 4 <= wm; k += 4) {
+        VT v0[4], v1[4];
+        int c0[4], c1[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v0[u] = __ldcs(vp0 + 32 * (k + u));
+            c0[u] = __ldcs(cp0 + 32 * (k + u));
+            v1[u] = __ldcs(vp1 + 32 * (k + u));
+            c1[u] = __ldcs(cp1 + 32 * (k + u));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a0 = fma((AccT)v0[u], (AccT)P[c0[u]], a0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a1 = fma((AccT)v1[u], (AccT)P[c1[u]], a1);
+    }
+    int k0 = k, k1 = k;
+    for (; k0 + 4 <= w0; k0 += 4) {
+        VT v[4];
+        int c[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[u] = __ldcs(vp0 + 32 * (k0 + u));
+            c[u] = __ldcs(cp0 + 32 * (k0 + u));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a0 = fma((AccT)v[u], (AccT)P[c[u]], a0);
+    }
+    for (; k1 + 4 <= w1; k1 += 4) {
+        VT v[4];
+        int c[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[u] = __ldcs(vp1 + 32 * (k1 + u));
+            c[u] = __ldcs(cp1 + 32 * (k1 + u));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a1 = fma((AccT)v[u], (AccT)P[c[u]], a1);
+    }
+    // the last w mod 4 columns of both slices, interleaved where both have one
+    for (; k0 < w0 || k1 < w1; ++k0, ++k1) {
+        const bool h0 = k0 < w0, h1 = k1 < w1;
+        VT v0 = VT(0), v1 = VT(0);
+        int c0 = 0, c1 = 0;
+        if (h0) {
+            v0 = __ldcs(vp0 + 32 * k0);
+            c0 = __ldcs(cp0 + 32 * k0);
+        }
+        if (h1) {
+            v1 = __ldcs(vp1 + 32 * k1);
+            c1 = __ldcs(cp1 + 32 * k1);
+        }
+        if (h0) a0 = fma((AccT)v0, (AccT)P[c0], a0);
+        if (h1) a1 = fma((AccT)v1, (AccT)P[c1], a1);
+    }
+    acc0 = a0;
+    acc1 = a1;
+}
+
+// Elements per step of the update and p-update passes (loads first).  On
+// 4,096 systems the fp64 batch took 156.2 / 149.8 / 148.0 ms with 1 / 2 / 4.
+constexpr int kBatchUpd = 4;
+
 // CTA sum returned in every thread.  Doubles: the narrow block_allsum, in
 // which warp 0 alone adds the threads' values in a fixed order
-// (xjpcg_device.cuh), so few FP64 adds are spent.  The FP64 kernel pins three
-// 512-thread CTAs per SM (1,536 threads) in its launch bounds: left to the
-// compiler, the narrow sum's lower register count moved it to four CTAs with
-// spills, which measured slower than a shuffle tree (190 against 176 ms for
-// 4,096 systems); pinned, it measures 172 ms.  Floats (the mixed kernel's
+// (xjpcg_device.cuh), so few FP64 adds are spent.  The FP64 kernel pins its
+// CTAs per SM in its launch bounds: left to the compiler, the narrow sum's
+// lower register count moved it to four CTAs with spills, which measured
+// slower than a shuffle tree (190 against 176 ms for 4,096 systems).  Floats (the mixed kernel's
 // inner sums): a shuffle tree in every warp, which costs no FP64 work and
 // keeps the serial chain of warp 0 off the critical path (111.5 ms against
 // 122.5 ms with the narrow form).
@@ -218,7 +296,21 @@ __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const
         AccT pAp = 0;
         if (SL) {
             // warp w takes slices w, w + NT/32, ...: 32 rows, one per lane
-            for (int j = tid >> 5; 32 * j < n; j += NT / 32) {
+            int j = tid >> 5;
+            for (; 32 * (j + NT / 32) < n; j += 2 * (NT / 32)) {
+                AccT acc0, acc1;
+                slice_dot2<VT, AccT>(sliceOff, j, j + NT / 32, sval, scol, P, tid & 31, acc0, acc1);
+                const int row0 = 32 * j + (tid & 31), row1 = row0 + NT;
+                if (row0 < n) {
+                    Ap[row0] = (VT)acc0;
+                    pAp = fma((AccT)P[row0], acc0, pAp);
+                }
+                if (row1 < n) {
+                    Ap[row1] = (VT)acc1;
+                    pAp = fma((AccT)P[row1], acc1, pAp);
+                }
+            }
+            for (; 32 * j < n; j += NT / 32) {
                 const AccT acc = slice_dot<VT, AccT>(sliceOff, j, sval, scol, P, tid & 31);
                 const int row = 32 * j + (tid & 31);
                 if (row < n) {
@@ -249,13 +341,39 @@ __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const
         const double alphaD = block_allreduce_q<NT, 1, 0, true>(v1, rz);  // rz / p.Ap
         const VT alpha = (VT)alphaD;
         AccT rrP = 0, rzP = 0;
-        for (int i = tid; i < n; i += NT) {
+        // kBatchUpd elements per step, all loads first: the vectors stream
+        // from DRAM, and one element's loads alone leave the warp waiting on
+        // them.  The sums still take the elements in the order i, i + NT, ...
+        constexpr int UPD = kBatchUpd;
+        int i = tid;
+        for (; i + (UPD - 1) * NT < n; i += UPD * NT) {
+            VT pv[UPD], dv[UPD], av[UPD], qv[UPD], jv[UPD];
+#pragma unroll
+            for (int u = 0; u < UPD; ++u) {
+                pv[u] = P[i + u * NT];
+                dv[u] = d[i + u * NT];
+                av[u] = Ap[i + u * NT];
+                qv[u] = r[i + u * NT];
+                jv[u] = J[i + u * NT];
+            }
+#pragma unroll
+            for (int u = 0; u < UPD; ++u) {
+                const VT ri = fma(-alpha, av[u], qv[u]);
+                const VT zi = ri * jv[u];
+                d[i + u * NT] = fma(alpha, pv[u], dv[u]);
+                r[i + u * NT] = ri;
+                Ap[i + u * NT] = zi;  // Ap is spent: keep z = J r for the p update
+                rrP = fma((AccT)ri, (AccT)ri, rrP);
+                rzP = fma((AccT)ri, (AccT)zi, rzP);
+            }
+        }
+        for (; i < n; i += NT) {
             const VT di = fma(alpha, P[i], d[i]);
             const VT ri = fma(-alpha, Ap[i], r[i]);
             const VT zi = ri * J[i];
             d[i] = di;
             r[i] = ri;
-            Ap[i] = zi;  // Ap is spent: keep z = J r for the p update
+            Ap[i] = zi;
             rrP = fma((AccT)ri, (AccT)ri, rrP);
             rzP = fma((AccT)ri, (AccT)zi, rzP);
         }
@@ -270,7 +388,18 @@ __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const
         }
         if (!(w[0] >= tols) || k >= maxK) break;  // !(rr >= tols) == (rr < tols) or NaN (caught above)
         const VT betaV = (VT)beta;
-        for (int i = tid; i < n; i += NT) P[i] = fma(betaV, P[i], Ap[i]);  // z + beta p, z = J r
+        int t = tid;
+        for (; t + (UPD - 1) * NT < n; t += UPD * NT) {  // z + beta p, z = J r
+            VT pv[UPD], zv[UPD];
+#pragma unroll
+            for (int u = 0; u < UPD; ++u) {
+                pv[u] = P[t + u * NT];
+                zv[u] = Ap[t + u * NT];
+            }
+#pragma unroll
+            for (int u = 0; u < UPD; ++u) P[t + u * NT] = fma(betaV, pv[u], zv[u]);
+        }
+        for (; t < n; t += NT) P[t] = fma(betaV, P[t], Ap[t]);
         __syncthreads();
     }
     return k;
@@ -286,8 +415,12 @@ __device__ __forceinline__ int next_system(const BatchArgs& a) {
     return t < a.nsys ? a.order[t] : -1;
 }
 
+// Launch bounds of 1,024 threads per SM (two 512-thread CTAs, 64 registers):
+// the interleaved slices and the 4-element passes keep their loads in
+// registers.  Pinned at 1,536 threads (40 registers) the same code spilled and
+// the 4,096-system batch took 155.5 ms against 148.0 ms.
 template <int NT, int G, bool SL>
-__global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_fp64_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(NT, (1024 / NT) > 0 ? 1024 / NT : 1) batched_fp64_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     double* pS = reinterpret_cast<double*>(smem);
     for (;;) {
@@ -330,8 +463,10 @@ __global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_f
 // spent, the refresh folds d into the FP64 x, recomputes r = b - A x with the
 // FP64 matrix and restarts the FP32 residual from it.  The system stops on the
 // true FP64 residual: r.r <= b.b tol^2.
+// Launch bounds of 1,536 threads per SM (three 512-thread CTAs, 40 registers,
+// no spills): 80.9 ms on 4,096 systems, against 95.8 ms at two CTAs per SM.
 template <int NT, int G, bool SL>
-__global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_mixed_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* pS = reinterpret_cast<float*>(smem);
     const int tid = threadIdx.x;
@@ -378,7 +513,21 @@ __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
             float pAp = 0.f;
             if (SL) {
                 const int* so = a.sliceOff + a.sliceBase[sys];
-                for (int j = tid >> 5; 32 * j < n; j += NT / 32) {
+                int j = tid >> 5;
+                for (; 32 * (j + NT / 32) < n; j += 2 * (NT / 32)) {
+                    float acc0, acc1;
+                    slice_dot2<float, float>(so, j, j + NT / 32, a.sval32, a.scol, P, tid & 31, acc0, acc1);
+                    const int row0 = 32 * j + (tid & 31), row1 = row0 + NT;
+                    if (row0 < n) {
+                        Ap[row0] = acc0;
+                        pAp = fmaf(P[row0], acc0, pAp);
+                    }
+                    if (row1 < n) {
+                        Ap[row1] = acc1;
+                        pAp = fmaf(P[row1], acc1, pAp);
+                    }
+                }
+                for (; 32 * j < n; j += NT / 32) {
                     const float acc = slice_dot<float, float>(so, j, a.sval32, a.scol, P, tid & 31);
                     const int row = 32 * j + (tid & 31);
                     if (row < n) {
@@ -409,7 +558,30 @@ __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
             const double alphaD = rz / (double)v1[0];
             const float alpha = (float)alphaD;
             float rrP = 0.f, rzP = 0.f;
-            for (int i = tid; i < n; i += NT) {
+            constexpr int UPDM = kBatchUpd;
+            int i = tid;
+            for (; i + (UPDM - 1) * NT < n; i += UPDM * NT) {
+                float pv[UPDM], dv[UPDM], av[UPDM], qv[UPDM], jv[UPDM];
+#pragma unroll
+                for (int u = 0; u < UPDM; ++u) {
+                    pv[u] = P[i + u * NT];
+                    dv[u] = d[i + u * NT];
+                    av[u] = Ap[i + u * NT];
+                    qv[u] = r[i + u * NT];
+                    jv[u] = J[i + u * NT];
+                }
+#pragma unroll
+                for (int u = 0; u < UPDM; ++u) {
+                    const float ri = fmaf(-alpha, av[u], qv[u]);
+                    const float zi = ri * jv[u];
+                    d[i + u * NT] = fmaf(alpha, pv[u], dv[u]);
+                    r[i + u * NT] = ri;
+                    Ap[i + u * NT] = zi;
+                    rrP = fmaf(ri, ri, rrP);
+                    rzP = fmaf(ri, zi, rzP);
+                }
+            }
+            for (; i < n; i += NT) {
                 const float ri = fmaf(-alpha, Ap[i], r[i]);
                 const float zi = ri * J[i];
                 d[i] = fmaf(alpha, P[i], d[i]);
@@ -467,7 +639,18 @@ __global__ void __launch_bounds__(NT) batched_mixed_kernel(BatchArgs a) {
             }
             if (stop) break;
             const float betaF = (float)beta;
-            for (int i = tid; i < n; i += NT) P[i] = fmaf(betaF, P[i], Ap[i]);  // z + beta p
+            int t = tid;
+            for (; t + (UPDM - 1) * NT < n; t += UPDM * NT) {  // z + beta p
+                float pv[UPDM], zv[UPDM];
+#pragma unroll
+                for (int u = 0; u < UPDM; ++u) {
+                    pv[u] = P[t + u * NT];
+                    zv[u] = Ap[t + u * NT];
+                }
+#pragma unroll
+                for (int u = 0; u < UPDM; ++u) P[t + u * NT] = fmaf(betaF, pv[u], zv[u]);
+            }
+            for (; t < n; t += NT) P[t] = fmaf(betaF, P[t], Ap[t]);  // z + beta p
             __syncthreads();
         }
         if (tid == 0) {
