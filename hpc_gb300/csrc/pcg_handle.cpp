@@ -1785,11 +1785,17 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
     }
 
     // Shape candidates: CTA size x lanes per row x rows of p kept in shared
-    // memory (the largest system, or a third of it for more CTAs per SM).
+    // memory: the largest system (up to 200 KB), 4,096 rows, or 44 KB.  More
+    // shared memory leaves less L1 for the matrix and the vectors: on 4,096
+    // systems the fp64 batch took 148.1 / 149.6 / 171.8 ms with 4,096 / 8,192 /
+    // 11,264 rows, and the mixed one 81.6 / 78.8 ms with 4,096 / 11,264 rows.
     const size_t esz = mixed ? sizeof(float) : sizeof(double);
     const int smemCap = (int)(200 * 1024 / esz);
-    std::vector<int> smemRows = {std::min(maxN, smemCap), std::min(maxN, 4096)};
-    if (smemRows[1] == smemRows[0]) smemRows.pop_back();
+    std::vector<int> smemRows;
+    for (int rows : {smemCap, 4096, (int)(44 * 1024 / esz)}) {
+        rows = std::min(maxN, rows);
+        if (std::find(smemRows.begin(), smemRows.end(), rows) == smemRows.end()) smemRows.push_back(rows);
+    }
     const uint64_t key = mixKey(mixKey(mixKey(nsys, (uint64_t)total), (uint64_t)nnz),
                                 (uint64_t)precision + 7 + (sliced ? 1000 : 0));
     const int forced = envInt("XJPCG_BATCH_CFG", -1);
