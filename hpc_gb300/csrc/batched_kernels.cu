@@ -96,6 +96,26 @@ __device__ __forceinline__ AccT slice_dot(const int* __restrict__ sliceOff, int 
     return acc;
 }
 
+// R remaining columns of two slices as one batch: all loads, then the
+// gathers, then each slice's FMAs in column order.
+template <int R, typename VT, typename AccT>
+__device__ __forceinline__ void slice_tail2(const VT* vp0, const uint16_t* cp0, const VT* vp1,
+                                            const uint16_t* cp1, int k0, int k1, const VT* P, AccT& a0, AccT& a1) {
+    VT v0[R], v1[R];
+    int c0[R], c1[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+        v0[u] = __ldcs(vp0 + 32 * (k0 + u));
+        c0[u] = __ldcs(cp0 + 32 * (k0 + u));
+        v1[u] = __ldcs(vp1 + 32 * (k1 + u));
+        c1[u] = __ldcs(cp1 + 32 * (k1 + u));
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) a0 = fma((AccT)v0[u], (AccT)P[c0[u]], a0);
+#pragma unroll
+    for (int u = 0; u < R; ++u) a1 = fma((AccT)v1[u], (AccT)P[c1[u]], a1);
+}
+
 // Two slices of one warp at once (j0 and j1), for twice the loads in flight:
 // their batches of 4 columns are interleaved while both slices have one, then
 // each slice finishes alone.  Each slice's FMAs run in its column order, as in
@@ -151,7 +171,19 @@ __device__ __forceinline__ void slice_dot2(const int* __restrict__ sliceOff, int
 #pragma unroll
         for (int u = 0; u < 4; ++u) a1 = fma((AccT)v[u], (AccT)P[c[u]], a1);
     }
-    // the last w mod 4 columns of both slices, interleaved where both have one
+    // the last w mod 4 columns: one unrolled batch when both slices have the
+    // same number left (the usual case: equal widths), else column by column
+    if (w0 - k0 == w1 - k1) {
+        switch (w0 - k0) {
+            case 1: slice_tail2<1>(vp0, cp0, vp1, cp1, k0, k1, P, a0, a1); break;
+            case 2: slice_tail2<2>(vp0, cp0, vp1, cp1, k0, k1, P, a0, a1); break;
+            case 3: slice_tail2<3>(vp0, cp0, vp1, cp1, k0, k1, P, a0, a1); break;
+            default: break;
+        }
+        acc0 = a0;
+        acc1 = a1;
+        return;
+    }
     for (; k0 < w0 || k1 < w1; ++k0, ++k1) {
         const bool h0 = k0 < w0, h1 = k1 < w1;
         VT v0 = VT(0), v1 = VT(0);
