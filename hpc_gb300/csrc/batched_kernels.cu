@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdint>
 #include <type_traits>
 
@@ -70,6 +71,8 @@ struct BatchArgs {
     const double* sval;
     const float* sval32;
     const uint16_t* scol;
+    const int* patLen;  // per global slice: shared column offsets, or 0
+    const int* patOff;  // kBatchPatMax per global slice
 };
 
 // One sliced row sum: lane l of the warp holds row 32 j + l of its system.
@@ -96,6 +99,18 @@ __device__ __forceinline__ AccT slice_dot(const int* __restrict__ sliceOff, int 
     return acc;
 }
 
+// Which kernels read shared column offsets (slice_dot2's first branch).  On
+// 4,096 systems (same iterations, same bits either way): mixed 71.7 ms
+// against 77.1 ms without; fp64 143.4 ms against 142.0 ms without, where the
+// slice's pattern length is one more dependent load before the values.
+constexpr bool kBatchPat64 = false;
+constexpr bool kBatchPat32 = true;
+
+// Slice pairs of equal width up to this many columns take all their columns
+// in one batch (fp64 kernel; at 40 registers the mixed kernel spilled).  On
+// 4,096 systems: 143.7 / 143.4 / 142.3 ms with none / up to 5 / up to 7.
+constexpr int kBatchOne = 7;
+
 // R remaining columns of two slices as one batch: all loads, then the
 // gathers, then each slice's FMAs in column order.
 template <int R, typename VT, typename AccT>
@@ -116,14 +131,62 @@ __device__ __forceinline__ void slice_tail2(const VT* vp0, const uint16_t* cp0, 
     for (int u = 0; u < R; ++u) a1 = fma((AccT)v1[u], (AccT)P[c1[u]], a1);
 }
 
+// Two slices with shared column offsets, R columns each, as one batch: the
+// offsets come from the slices' small tables (one cached line for the warp),
+// so the gathers x[row + o] need no column load from DRAM and go out with the
+// value loads.  FMAs in column order, as in slice_dot.
+template <int R, typename VT, typename AccT>
+__device__ __forceinline__ void slice_pat2(const VT* vp0, const VT* vp1, const int* __restrict__ po0,
+                                           const int* __restrict__ po1, const VT* x0, const VT* x1, AccT& a0,
+                                           AccT& a1) {
+    VT v0[R], v1[R];
+    int o0[R], o1[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+        v0[u] = __ldcs(vp0 + 32 * u);
+        v1[u] = __ldcs(vp1 + 32 * u);
+        o0[u] = __ldg(po0 + u);
+        o1[u] = __ldg(po1 + u);
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) a0 = fma((AccT)v0[u], (AccT)x0[o0[u]], a0);
+#pragma unroll
+    for (int u = 0; u < R; ++u) a1 = fma((AccT)v1[u], (AccT)x1[o1[u]], a1);
+}
+
 // Two slices of one warp at once (j0 and j1), for twice the loads in flight:
 // their batches of 4 columns are interleaved while both slices have one, then
 // each slice finishes alone.  Each slice's FMAs run in its column order, as in
 // slice_dot, so both sums are slice_dot's bit for bit.
-template <typename VT, typename AccT>
-__device__ __forceinline__ void slice_dot2(const int* __restrict__ sliceOff, int j0, int j1,
+template <typename VT, typename AccT, int ONE, bool PAT>
+__device__ __forceinline__ void slice_dot2(const int* __restrict__ sliceOff, const int* __restrict__ patLen,
+                                           const int* __restrict__ patOff, int j0, int j1,
                                            const VT* __restrict__ sval, const uint16_t* __restrict__ scol,
                                            const VT* P, int lane32, AccT& acc0, AccT& acc1) {
+    if (PAT) {
+        const int L0 = patLen[j0], L1 = patLen[j1];
+        if (L0 > 0 && L0 == L1 && L0 <= 7) {
+            const VT* vp0 = sval + sliceOff[j0] + lane32;
+            const VT* vp1 = sval + sliceOff[j1] + lane32;
+            const int* po0 = patOff + (size_t)j0 * kBatchPatMax;
+            const int* po1 = patOff + (size_t)j1 * kBatchPatMax;
+            const VT* x0 = P + 32 * j0 + lane32;
+            const VT* x1 = P + 32 * j1 + lane32;
+            AccT a0 = AccT(0), a1 = AccT(0);
+            switch (L0) {
+                case 1: slice_pat2<1>(vp0, vp1, po0, po1, x0, x1, a0, a1); break;
+                case 2: slice_pat2<2>(vp0, vp1, po0, po1, x0, x1, a0, a1); break;
+                case 3: slice_pat2<3>(vp0, vp1, po0, po1, x0, x1, a0, a1); break;
+                case 4: slice_pat2<4>(vp0, vp1, po0, po1, x0, x1, a0, a1); break;
+                case 5: slice_pat2<5>(vp0, vp1, po0, po1, x0, x1, a0, a1); break;
+                case 6: slice_pat2<6>(vp0, vp1, po0, po1, x0, x1, a0, a1); break;
+                default: slice_pat2<7>(vp0, vp1, po0, po1, x0, x1, a0, a1); break;
+            }
+            acc0 = a0;
+            acc1 = a1;
+            return;
+        }
+    }
     const int off0 = sliceOff[j0], w0 = (sliceOff[j0 + 1] - off0) >> 5;
     const int off1 = sliceOff[j1], w1 = (sliceOff[j1 + 1] - off1) >> 5;
     const VT* vp0 = sval + off0 + lane32;
@@ -131,6 +194,22 @@ __device__ __forceinline__ void slice_dot2(const int* __restrict__ sliceOff, int
     const uint16_t* cp0 = scol + off0 + lane32;
     const uint16_t* cp1 = scol + off1 + lane32;
     AccT a0 = AccT(0), a1 = AccT(0);
+    if (ONE > 0 && w0 == w1 && w0 <= ONE) {
+        // narrow slices (a 5-point stencil): every column in one batch
+        switch (w0) {
+            case 1: slice_tail2<1>(vp0, cp0, vp1, cp1, 0, 0, P, a0, a1); break;
+            case 2: slice_tail2<2>(vp0, cp0, vp1, cp1, 0, 0, P, a0, a1); break;
+            case 3: slice_tail2<3>(vp0, cp0, vp1, cp1, 0, 0, P, a0, a1); break;
+            case 4: slice_tail2<4>(vp0, cp0, vp1, cp1, 0, 0, P, a0, a1); break;
+            case 5: slice_tail2<5>(vp0, cp0, vp1, cp1, 0, 0, P, a0, a1); break;
+            case 6: if (ONE >= 6) slice_tail2<6>(vp0, cp0, vp1, cp1, 0, 0, P, a0, a1); break;
+            case 7: if (ONE >= 7) slice_tail2<7>(vp0, cp0, vp1, cp1, 0, 0, P, a0, a1); break;
+            default: break;
+        }
+        acc0 = a0;
+        acc1 = a1;
+        return;
+    }
     const int wm = w0 < w1 ? w0 : w1;
     int k = 0;
     for (; k + 4 <= wm; k += 4) {
@@ -299,6 +378,7 @@ __device__ __forceinline__ double block_allreduce_q(double (&v)[NV], double num)
 template <typename VT, int NT, int G, bool SL>
 __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const int* __restrict__ col,
                             const VT* __restrict__ val, const int* __restrict__ sliceOff,
+                            const int* __restrict__ patLen, const int* __restrict__ patOff,
                             const VT* __restrict__ sval, const uint16_t* __restrict__ scol, VT* __restrict__ r,
                             VT* __restrict__ d, const VT* __restrict__ J, VT* __restrict__ Ap, VT* P, double relTol,
                             uint32_t maxK, double& rrLast, double& rr0Out, bool& breakdown) {
@@ -331,7 +411,8 @@ __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const
             int j = tid >> 5;
             for (; 32 * (j + NT / 32) < n; j += 2 * (NT / 32)) {
                 AccT acc0, acc1;
-                slice_dot2<VT, AccT>(sliceOff, j, j + NT / 32, sval, scol, P, tid & 31, acc0, acc1);
+                slice_dot2<VT, AccT, kBatchOne, kBatchPat64>(sliceOff, patLen, patOff, j, j + NT / 32, sval, scol, P,
+                                                                 tid & 31, acc0, acc1);
                 const int row0 = 32 * j + (tid & 31), row1 = row0 + NT;
                 if (row0 < n) {
                     Ap[row0] = (VT)acc0;
@@ -473,7 +554,9 @@ __global__ void __launch_bounds__(NT, (1024 / NT) > 0 ? 1024 / NT : 1) batched_f
         double rrLast, rr0;
         bool bd;
         const uint32_t k = cg_core<double, NT, G, SL>(
-            n, a.rowptr + r0, e0, a.col + e0, a.val + e0, SL ? a.sliceOff + a.sliceBase[sys] : nullptr, a.sval, a.scol,
+            n, a.rowptr + r0, e0, a.col + e0, a.val + e0, SL ? a.sliceOff + a.sliceBase[sys] : nullptr,
+            SL ? a.patLen + a.sliceBase[sys] : nullptr,
+            SL ? a.patOff + (size_t)a.sliceBase[sys] * kBatchPatMax : nullptr, a.sval, a.scol,
             a.r + r0, a.x + r0, a.J + r0, a.Ap + r0, P, a.tol, a.maxIterP1, rrLast, rr0, bd);
         if (threadIdx.x == 0) {
             BatchResult& o = a.res[sys];
@@ -548,7 +631,10 @@ __global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_m
                 int j = tid >> 5;
                 for (; 32 * (j + NT / 32) < n; j += 2 * (NT / 32)) {
                     float acc0, acc1;
-                    slice_dot2<float, float>(so, j, j + NT / 32, a.sval32, a.scol, P, tid & 31, acc0, acc1);
+                    slice_dot2<float, float, 0, kBatchPat32>(so, a.patLen + a.sliceBase[sys],
+                                                                     a.patOff + (size_t)a.sliceBase[sys] * kBatchPatMax,
+                                                                     j, j + NT / 32, a.sval32, a.scol, P, tid & 31,
+                                                                     acc0, acc1);
                     const int row0 = 32 * j + (tid & 31), row1 = row0 + NT;
                     if (row0 < n) {
                         Ap[row0] = acc0;
@@ -793,6 +879,12 @@ __device__ __forceinline__ int warp_max_i(int v) {
     return v;
 }
 
+__device__ __forceinline__ int warp_min_i(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
 // System of global slice g: the largest s with sliceBase[s] <= g.
 __device__ __forceinline__ int system_of_slice(const int* __restrict__ sliceBase, int nsys, int g) {
     int lo = 0, hi = nsys - 1;
@@ -808,28 +900,74 @@ __device__ __forceinline__ int system_of_slice(const int* __restrict__ sliceBase
 }  // namespace
 
 // One warp per slice: stored entries 32 x (the slice's longest row).
+// One warp per slice: the stored width, and whether the slice's rows share
+// their column offsets.  The shared form takes the union of the 32 rows'
+// offsets (column - row), in ascending order, as the slice's columns: row i's
+// entry with offset o sits at o's position and the other positions hold 0.
+// It is used when every row of the slice exists, every row's columns ascend
+// strictly, the union has at most kBatchPatMax offsets and row + o lies in
+// the system for all 32 rows and every o -- then each row's FMAs take its
+// entries in the same order as the plain form, with exact zeros between them
+// (adding +-0 to a sum that starts at +0 leaves it unchanged), and every
+// gather, padding included, stays inside the system.  len[g] = 32 x width;
+// patLen[g] = the number of shared offsets, or 0.  The union is built by
+// repeated warp minima over each row's next offset, at most kBatchPatMax + 1
+// steps.
 __global__ void bsell_width_kernel(int nsys, int nslices, const int* __restrict__ sysRow,
                                    const int* __restrict__ sliceBase, const int* __restrict__ rowptr,
-                                   int* __restrict__ len) {
+                                   const int* __restrict__ col, int* __restrict__ len, int* __restrict__ patLen,
+                                   int* __restrict__ patOff) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nslices; g += warps) {
         const int s = system_of_slice(sliceBase, nsys, g);
         const int r0 = sysRow[s], n = sysRow[s + 1] - r0;
-        const int lr = (g - sliceBase[s]) * 32 + lane;
-        const int rl = lr < n ? rowptr[r0 + lr + 1] - rowptr[r0 + lr] : 0;
-        const int w = warp_max_i(rl);
-        if (lane == 0) len[g] = 32 * w;
+        const int first = (g - sliceBase[s]) * 32;
+        const int lr = first + lane;
+        const bool in = lr < n;
+        const int j0 = in ? rowptr[r0 + lr] : 0, j1 = in ? rowptr[r0 + lr + 1] : 0;
+        const int w = warp_max_i(j1 - j0);
+        bool ok = __all_sync(0xffffffffu, in);
+        int L = 0, q = j0, myOff = 0;
+        int cur = q < j1 ? col[q] - lr : INT_MAX;
+        while (ok) {
+            const int m = warp_min_i(cur);
+            if (m == INT_MAX) break;
+            if (L == kBatchPatMax || first + m < 0 || first + 31 + m >= n) {
+                ok = false;
+                break;
+            }
+            if (lane == L) myOff = m;
+            ++L;
+            bool bad = false;
+            if (cur == m) {
+                ++q;
+                const int nx = q < j1 ? col[q] - lr : INT_MAX;
+                bad = nx <= m;  // not strictly ascending
+                cur = nx;
+            }
+            ok = !__any_sync(0xffffffffu, bad);
+        }
+        if (!ok) L = 0;
+        if (lane == 0) {
+            len[g] = 32 * (L > 0 ? L : w);
+            patLen[g] = L;
+        }
+        if (lane < kBatchPatMax) patOff[(size_t)g * kBatchPatMax + lane] = lane < L ? myOff : 0;
     }
 }
 
 // One warp per slice: values (and, when scol is given, local columns) in
-// slice-column-major order; padding entries hold value 0 and column 0.
+// slice-column-major order.  Plain slices: each row's entries in order, then
+// padding with value 0 and column 0.  Shared slices: each row's entries at
+// their offsets' positions, value 0 elsewhere, and column row + offset at
+// every position.
 template <typename VT>
 __global__ void bsell_fill_kernel(int nsys, int nslices, const int* __restrict__ sysRow,
                                   const int* __restrict__ sliceBase, const int* __restrict__ rowptr,
                                   const int* __restrict__ col, const double* __restrict__ val,
-                                  const int* __restrict__ sliceOff, VT* __restrict__ sval, uint16_t* __restrict__ scol) {
+                                  const int* __restrict__ sliceOff, const int* __restrict__ patLen,
+                                  const int* __restrict__ patOff, VT* __restrict__ sval, uint16_t* __restrict__ scol) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nslices; g += warps) {
@@ -838,6 +976,18 @@ __global__ void bsell_fill_kernel(int nsys, int nslices, const int* __restrict__
         const int lr = (g - sliceBase[s]) * 32 + lane;
         const int j0 = lr < n ? rowptr[r0 + lr] : 0, j1 = lr < n ? rowptr[r0 + lr + 1] : 0;
         const int off = sliceOff[g], w = (sliceOff[g + 1] - off) >> 5;
+        const int L = patLen[g];
+        if (L > 0) {
+            int q = j0;
+            for (int k = 0; k < L; ++k) {
+                const int o = patOff[(size_t)g * kBatchPatMax + k];
+                const bool has = q < j1 && col[q] - lr == o;
+                sval[off + 32 * k + lane] = has ? (VT)val[q] : VT(0);
+                if (scol) scol[off + 32 * k + lane] = (uint16_t)(lr + o);
+                if (has) ++q;
+            }
+            continue;
+        }
         for (int k = 0; k < w; ++k) {
             const bool has = j0 + k < j1;
             sval[off + 32 * k + lane] = has ? (VT)val[j0 + k] : VT(0);
@@ -847,9 +997,10 @@ __global__ void bsell_fill_kernel(int nsys, int nslices, const int* __restrict__
 }
 
 cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
-                              const int* rowptr, int* sliceLen, int* sliceOff, int* blockSums) {
+                              const int* rowptr, const int* col, int* sliceLen, int* sliceOff, int* blockSums,
+                              int* patLen, int* patOff) {
     const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, device_sm_count() * 32));
-    bsell_width_kernel<<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, sliceLen);
+    bsell_width_kernel<<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, col, sliceLen, patLen, patOff);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return scan_exclusive(st, sliceLen, sliceOff, nslices + 1, blockSums);
@@ -857,17 +1008,17 @@ cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int*
 
 template <typename VT>
 cudaError_t batch_sell_fill(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
-                            const int* rowptr, const int* col, const double* val, const int* sliceOff, VT* sval,
-                            uint16_t* scol) {
+                            const int* rowptr, const int* col, const double* val, const int* sliceOff,
+                            const int* patLen, const int* patOff, VT* sval, uint16_t* scol) {
     const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, device_sm_count() * 32));
-    bsell_fill_kernel<VT><<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, col, val, sliceOff, sval,
-                                                scol);
+    bsell_fill_kernel<VT><<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, col, val, sliceOff, patLen,
+                                                patOff, sval, scol);
     return cudaGetLastError();
 }
 template cudaError_t batch_sell_fill<double>(cudaStream_t, int, int, const int*, const int*, const int*, const int*,
-                                             const double*, const int*, double*, uint16_t*);
+                                             const double*, const int*, const int*, const int*, double*, uint16_t*);
 template cudaError_t batch_sell_fill<float>(cudaStream_t, int, int, const int*, const int*, const int*, const int*,
-                                            const double*, const int*, float*, uint16_t*);
+                                            const double*, const int*, const int*, const int*, float*, uint16_t*);
 
 // smemRows: rows of p kept in shared memory; systems larger than that keep p
 // in the global scratch vector (still correct, slower).
@@ -904,6 +1055,8 @@ cudaError_t batch_launch(int cfg, bool mixed, int numSms, int smemRows, cudaStre
     a.sval = L.sval;
     a.sval32 = L.sval32;
     a.scol = L.scol;
+    a.patLen = L.patLen;
+    a.patOff = L.patOff;
     const size_t smem = (size_t)smemRows * (mixed ? sizeof(float) : sizeof(double));
     const BatchCfg& c = kBatchCfgs[cfg];
     const int bps = c.bps(mixed, smem);

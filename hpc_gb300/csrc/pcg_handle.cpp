@@ -1709,7 +1709,8 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
     // every system has at most 65,536 rows and the copy fits 32-bit offsets.
     int64_t nslices = 0;
     for (uint32_t s = 0; s < nsys; ++s) nslices += (hSys[s + 1] - hSys[s] + 31) / 32;
-    const bool sliced = maxN <= 65536 && nslices * 32 * (int64_t)std::max(maxRowLen, 1) < 0x7fffff00ll &&
+    const bool sliced = maxN <= 65536 &&
+                        nslices * 32 * (int64_t)std::max(maxRowLen, kBatchPatMax) < 0x7fffff00ll &&
                         envInt("XJPCG_BATCH_SLICED", 1) != 0;
     if (sliced) {
         const int nsl = (int)nslices;
@@ -1719,12 +1720,15 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
         alloc(m_bsLen, sizeof(int32_t) * ((size_t)nsl + 1), "batch slice lengths");
         alloc(m_bsOff, sizeof(int32_t) * ((size_t)nsl + 1), "batch slice offsets");
         alloc(m_bsScan, sizeof(int32_t) * ((size_t)scan_block_count(nsl + 1) + 1), "scan scratch");
+        alloc(m_bsPatLen, sizeof(int32_t) * ((size_t)nsl + 1), "batch slice patterns");
+        alloc(m_bsPatOff, sizeof(int32_t) * (size_t)kBatchPatMax * ((size_t)nsl + 1), "batch slice offsets");
         check(cudaMemcpyAsync(m_bsBase.p, hBase.data(), sizeof(int32_t) * (nsys + 1), cudaMemcpyHostToDevice,
                               m_stream),
               "H2D");
         check(cudaMemsetAsync(m_bsLen.p, 0, sizeof(int32_t) * ((size_t)nsl + 1), m_stream), "memset");
         check(batch_sell_widths(m_stream, (int)nsys, nsl, m_bSysRow.as<int>(), m_bsBase.as<int>(),
-                                m_bRowptr.as<int>(), m_bsLen.as<int>(), m_bsOff.as<int>(), m_bsScan.as<int>()),
+                                m_bRowptr.as<int>(), m_bCol.as<int>(), m_bsLen.as<int>(), m_bsOff.as<int>(),
+                                m_bsScan.as<int>(), m_bsPatLen.as<int>(), m_bsPatOff.as<int>()),
               "batch slices");
         int stored = 0;
         check(cudaMemcpyAsync(&stored, m_bsOff.as<int>() + nsl, sizeof(int), cudaMemcpyDeviceToHost, m_stream),
@@ -1735,13 +1739,15 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
             alloc(m_bsVal32, sizeof(float) * ((size_t)stored + 32), "batch sliced fp32 values");
             check(batch_sell_fill<float>(m_stream, (int)nsys, nsl, m_bSysRow.as<int>(), m_bsBase.as<int>(),
                                          m_bRowptr.as<int>(), m_bCol.as<int>(), m_bVal.as<double>(), m_bsOff.as<int>(),
-                                         m_bsVal32.as<float>(), m_bsCol.as<uint16_t>()),
+                                         m_bsPatLen.as<int>(), m_bsPatOff.as<int>(), m_bsVal32.as<float>(),
+                                         m_bsCol.as<uint16_t>()),
                   "batch sliced fp32 fill");
         } else {
             alloc(m_bsVal, sizeof(double) * ((size_t)stored + 32), "batch sliced values");
             check(batch_sell_fill<double>(m_stream, (int)nsys, nsl, m_bSysRow.as<int>(), m_bsBase.as<int>(),
                                           m_bRowptr.as<int>(), m_bCol.as<int>(), m_bVal.as<double>(),
-                                          m_bsOff.as<int>(), m_bsVal.as<double>(), m_bsCol.as<uint16_t>()),
+                                          m_bsOff.as<int>(), m_bsPatLen.as<int>(), m_bsPatOff.as<int>(),
+                                          m_bsVal.as<double>(), m_bsCol.as<uint16_t>()),
                   "batch sliced fill");
         }
     }
@@ -1782,6 +1788,8 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
         L.sval = mixed ? nullptr : m_bsVal.as<double>();
         L.sval32 = mixed ? m_bsVal32.as<float>() : nullptr;
         L.scol = m_bsCol.as<uint16_t>();
+        L.patLen = m_bsPatLen.as<int>();
+        L.patOff = m_bsPatOff.as<int>();
     }
 
     // Shape candidates: CTA size x lanes per row x rows of p kept in shared

@@ -207,18 +207,24 @@ struct BatchLaunch {
     const double* sval = nullptr;
     const float* sval32 = nullptr;
     const uint16_t* scol = nullptr;
+    const int* patLen = nullptr;  // per slice: shared column offsets, or 0
+    const int* patOff = nullptr;  // kBatchPatMax per slice
 };
 int batch_num_configs();
 cudaError_t batch_validate_columns(cudaStream_t st, int nsys, const int* sysRow, const int* rowptr, const int* col,
                                    int* flag);
 void batch_config_shape(int cfg, int* threads, int* lanes);
 bool batch_config_sliced(int cfg);  // the kernel reads the per-system SELL-32 copy
+// Shared column offsets per slice of the batched SELL-32 copy: at most this
+// many, stored kBatchPatMax ints per slice.
+constexpr int kBatchPatMax = 8;
 cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
-                              const int* rowptr, int* sliceLen, int* sliceOff, int* blockSums);
+                              const int* rowptr, const int* col, int* sliceLen, int* sliceOff, int* blockSums,
+                              int* patLen, int* patOff);
 template <typename VT>
 cudaError_t batch_sell_fill(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
-                            const int* rowptr, const int* col, const double* val, const int* sliceOff, VT* sval,
-                            uint16_t* scol);
+                            const int* rowptr, const int* col, const double* val, const int* sliceOff,
+                            const int* patLen, const int* patOff, VT* sval, uint16_t* scol);
 cudaError_t batch_launch(int cfg, bool mixed, int numSms, int smemRows, cudaStream_t st, const BatchLaunch& L,
                          int* gridOut);
 

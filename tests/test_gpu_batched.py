@@ -82,3 +82,56 @@ def test_batched_rejects_bad_columns(handle, batch):
     bad[1].col[3] = bad[1].n  # outside its own system
     st, _, _ = handle.batch_solve(bad, 100, 1e-10)
     assert st == X.INVALID_VALUE
+
+
+def _irregular_batch():
+    """Systems whose 32-row slices cannot all share column offsets: rows with
+    shuffled column order, a random banded SPD matrix with more than 8 offsets
+    per slice, systems shorter than a slice or not a multiple of 32 rows, next
+    to plain stencils whose first and last slices reach outside the system."""
+    rng = np.random.default_rng(11)
+    out = []
+    st = W.batched_stencils(count=6, lo=300, hi=3000, seed=5)
+    for k, s in enumerate(st):
+        if k % 2 == 0:
+            # the same matrix, each row's entries in a random order
+            col, val = s.col.copy(), s.val.copy()
+            for i in range(s.n):
+                a, b = s.rowptr[i], s.rowptr[i + 1]
+                p = rng.permutation(b - a)
+                col[a:b], val[a:b] = col[a:b][p], val[a:b][p]
+            s = W.System(s.n, s.rowptr, col, val, s.diag, s.b, s.name + "_shuffled")
+        out.append(s)
+    for n, band, dens in ((300, 24, 0.4), (17, 5, 0.6), (45, 9, 0.5), (97, 40, 0.2)):
+        a = np.zeros((n, n))
+        for i in range(n):
+            for j in range(max(0, i - band), i):
+                if rng.random() < dens:
+                    a[i, j] = a[j, i] = rng.normal()
+        np.fill_diagonal(a, np.abs(a).sum(1) * 1.05 + 0.5)
+        rows, cols = np.nonzero(a)
+        rowptr = np.zeros(n + 1, np.int32)
+        np.add.at(rowptr, rows + 1, 1)
+        rowptr = np.cumsum(rowptr).astype(np.int32)
+        out.append(W.System(n, rowptr, cols.astype(np.int32), a[rows, cols], np.diag(a).copy(),
+                            rng.uniform(-1, 1, n), "banded_%d" % n))
+    return out
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_sliced_irregular_slices(handle, precision, monkeypatch):
+    # the sliced shapes on slices that fall back to per-entry columns (and on
+    # the shared-offset slices beside them) meet the bar in both precisions
+    sub = _irregular_batch()
+    refs = [oracle.jpcg(s.rowptr, s.col, s.val, s.diag, s.b, 20000, 1e-10) for s in sub]
+    for cfg in (6, 7, 8):
+        monkeypatch.setenv("XJPCG_BATCH_CFG", str(cfg))
+        st, xs, res = handle.batch_solve(sub, 20000, 1e-10, precision=precision)
+        assert st == X.SUCCESS, (cfg, handle.last_message())
+        assert handle.info().batchSliced == 1
+        for s, x, r, ref in zip(sub, xs, res, refs):
+            assert r["status"] == 0, (cfg, s.name)
+            assert oracle.true_relres(s.rowptr, s.col, s.val, s.b, x) <= 1.5e-10, (cfg, s.name)
+            if precision == 0:
+                assert abs(int(r["iters"]) - ref["iters"]) <= max(1, int(0.01 * ref["iters"])), (cfg, s.name)
+                assert np.linalg.norm(x - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"]), (cfg, s.name)
