@@ -1730,6 +1730,12 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
                                 m_bRowptr.as<int>(), m_bCol.as<int>(), m_bsLen.as<int>(), m_bsOff.as<int>(),
                                 m_bsScan.as<int>(), m_bsPatLen.as<int>(), m_bsPatOff.as<int>()),
               "batch slices");
+        alloc(m_bsMeta, sizeof(int32_t) * 2 * ((size_t)nsl + 1), "batch slice records");
+        alloc(m_bsSysPat, sizeof(int32_t) * (size_t)(kBatchPatMax + 1) * (nsys + 1), "batch system offsets");
+        check(batch_sell_meta(m_stream, (int)nsys, nsl, m_bSysRow.as<int>(), m_bsBase.as<int>(), m_bsOff.as<int>(),
+                              m_bsPatLen.as<int>(), m_bsPatOff.as<int>(), static_cast<int2*>(m_bsMeta.p),
+                              m_bsSysPat.as<int>()),
+              "batch slice records");
         int stored = 0;
         check(cudaMemcpyAsync(&stored, m_bsOff.as<int>() + nsl, sizeof(int), cudaMemcpyDeviceToHost, m_stream),
               "D2H");
@@ -1790,6 +1796,8 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
         L.scol = m_bsCol.as<uint16_t>();
         L.patLen = m_bsPatLen.as<int>();
         L.patOff = m_bsPatOff.as<int>();
+        L.meta = static_cast<const int2*>(m_bsMeta.p);
+        L.sysPat = m_bsSysPat.as<int>();
     }
 
     // Shape candidates: CTA size x lanes per row x rows of p kept in shared

@@ -305,6 +305,7 @@ class PcgHandle {
     DevBuf m_bR32, m_bD32, m_bAp32, m_bJ32, m_bP, m_bP32, m_bRes, m_bQueue;
     DevBuf m_bsBase, m_bsLen, m_bsOff, m_bsScan, m_bsVal, m_bsVal32, m_bsCol;  // per-system SELL-32 copy
     DevBuf m_bsPatLen, m_bsPatOff;  // its slices' shared column offsets
+    DevBuf m_bsMeta, m_bsSysPat;    // slice records, and each system's offsets
     int m_batchCfg = -1, m_batchSmemRows = 0, m_batchGrid = 0;
     uint64_t m_batchKey = 0;
     float m_batchMs = 0.f;

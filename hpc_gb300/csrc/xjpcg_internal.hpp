@@ -209,6 +209,8 @@ struct BatchLaunch {
     const uint16_t* scol = nullptr;
     const int* patLen = nullptr;  // per slice: shared column offsets, or 0
     const int* patOff = nullptr;  // kBatchPatMax per slice
+    const int2* meta = nullptr;   // per slice: {value offset, width | kSliceSysPat}
+    const int* sysPat = nullptr;  // per system: pattern length, then kBatchPatMax offsets
 };
 int batch_num_configs();
 cudaError_t batch_validate_columns(cudaStream_t st, int nsys, const int* sysRow, const int* rowptr, const int* col,
@@ -218,6 +220,10 @@ bool batch_config_sliced(int cfg);  // the kernel reads the per-system SELL-32 c
 // Shared column offsets per slice of the batched SELL-32 copy: at most this
 // many, stored kBatchPatMax ints per slice.
 constexpr int kBatchPatMax = 8;
+// Flag in a slice record's width word: the slice uses its system's offsets.
+constexpr int kSliceSysPat = 1 << 30;
+cudaError_t batch_sell_meta(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
+                            const int* sliceOff, const int* patLen, const int* patOff, int2* meta, int* sysPat);
 cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
                               const int* rowptr, const int* col, int* sliceLen, int* sliceOff, int* blockSums,
                               int* patLen, int* patOff);
