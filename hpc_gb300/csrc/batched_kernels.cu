@@ -107,10 +107,12 @@ __device__ __forceinline__ AccT slice_dot(const int* __restrict__ sliceOff, int 
 // slice's pattern length is one more dependent load before the values.
 constexpr bool kBatchPat64 = false;
 constexpr bool kBatchPat32 = true;
-// The fp64 kernel's slice pairs that both use their system's offsets (held in
-// shared memory) gather without any dependent load but the slice record:
-// 138.1 ms against 142.0 ms with the columns, same bits.
+// Slice pairs that both use their system's offsets (held in shared memory)
+// gather without any dependent load but the slice record: fp64 138.1 ms
+// against 142.0 ms with the columns, mixed 65.0 ms against 71.5 ms with the
+// per-slice offsets; same bits.
 constexpr bool kBatchSys64 = true;
+constexpr bool kBatchSys32 = true;
 
 // Slice pairs of equal width up to this many columns take all their columns
 // in one batch (fp64 kernel; at 40 registers the mixed kernel spilled).  On
@@ -316,6 +318,40 @@ __device__ __forceinline__ void slice_dot2(const int* __restrict__ sliceOff, con
 // 4,096 systems the fp64 batch took 156.2 / 149.8 / 148.0 ms with 1 / 2 / 4.
 constexpr int kBatchUpd = 4;
 
+// Two slices j0 and j1 = j0 + stride/32 of one warp: by their system's
+// offsets when both records carry the flag (SYS), else slice_dot2.
+template <typename VT, typename AccT, int ONE, bool PAT, bool SYS>
+__device__ __forceinline__ void slice_pair(const int* __restrict__ sliceOff, const int* __restrict__ patLen,
+                                           const int* __restrict__ patOff, const int2* __restrict__ meta,
+                                           const int* sPat, int sysL, int j0, int j1, int stride,
+                                           const VT* __restrict__ sval, const uint16_t* __restrict__ scol,
+                                           const VT* P, int lane32, AccT& acc0, AccT& acc1) {
+    if (SYS && sysL > 0) {
+        const int2 m0 = meta[j0], m1 = meta[j1];
+        if (m0.y & m1.y & kSliceSysPat) {
+            const VT* vp0 = sval + m0.x + lane32;
+            const VT* vp1 = sval + m1.x + lane32;
+            const VT* x0 = P + 32 * j0 + lane32;
+            const VT* x1 = x0 + stride;
+            AccT a0 = AccT(0), a1 = AccT(0);
+            switch (sysL) {
+                case 1: slice_sys2<1>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
+                case 2: slice_sys2<2>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
+                case 3: slice_sys2<3>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
+                case 4: slice_sys2<4>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
+                case 5: slice_sys2<5>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
+                case 6: slice_sys2<6>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
+                case 7: slice_sys2<7>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
+                default: slice_sys2<8>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
+            }
+            acc0 = a0;
+            acc1 = a1;
+            return;
+        }
+    }
+    slice_dot2<VT, AccT, ONE, PAT>(sliceOff, patLen, patOff, j0, j1, sval, scol, P, lane32, acc0, acc1);
+}
+
 // CTA sum returned in every thread.  Doubles: the narrow block_allsum, in
 // which warp 0 alone adds the threads' values in a fixed order
 // (xjpcg_device.cuh), so few FP64 adds are spent.  The FP64 kernel pins its
@@ -443,33 +479,9 @@ __device__ uint32_t cg_core(int n, const int* __restrict__ rowptr, int e0, const
             const int sysL = kBatchSys64 ? sPat[0] : 0;  // the system's pattern length, 0: none
             for (; 32 * (j + NT / 32) < n; j += 2 * (NT / 32)) {
                 AccT acc0, acc1;
-                bool done = false;
-                if (kBatchSys64 && sysL > 0) {
-                    const int2 m0 = meta[j], m1 = meta[j + NT / 32];
-                    if (m0.y & m1.y & kSliceSysPat) {
-                        const VT* vp0 = sval + m0.x + (tid & 31);
-                        const VT* vp1 = sval + m1.x + (tid & 31);
-                        const VT* x0 = P + 32 * j + (tid & 31);
-                        const VT* x1 = x0 + NT;
-                        AccT a0 = AccT(0), a1 = AccT(0);
-                        switch (sysL) {
-                            case 1: slice_sys2<1>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
-                            case 2: slice_sys2<2>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
-                            case 3: slice_sys2<3>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
-                            case 4: slice_sys2<4>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
-                            case 5: slice_sys2<5>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
-                            case 6: slice_sys2<6>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
-                            case 7: slice_sys2<7>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
-                            default: slice_sys2<8>(vp0, vp1, sPat + 1, x0, x1, a0, a1); break;
-                        }
-                        acc0 = a0;
-                        acc1 = a1;
-                        done = true;
-                    }
-                }
-                if (!done)
-                    slice_dot2<VT, AccT, kBatchOne, kBatchPat64>(sliceOff, patLen, patOff, j, j + NT / 32, sval, scol,
-                                                                 P, tid & 31, acc0, acc1);
+                slice_pair<VT, AccT, kBatchOne, kBatchPat64, kBatchSys64>(sliceOff, patLen, patOff, meta, sPat, sysL, j,
+                                                                          j + NT / 32, NT, sval, scol, P, tid & 31,
+                                                                          acc0, acc1);
                 const int row0 = 32 * j + (tid & 31), row1 = row0 + NT;
                 if (row0 < n) {
                     Ap[row0] = (VT)acc0;
@@ -645,6 +657,7 @@ __global__ void __launch_bounds__(NT, (1024 / NT) > 0 ? 1024 / NT : 1) batched_f
 template <int NT, int G, bool SL>
 __global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_mixed_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int sPat[kBatchPatMax + 1];
     float* pS = reinterpret_cast<float*>(smem);
     const int tid = threadIdx.x;
     const int lane = tid % G;
@@ -654,6 +667,9 @@ __global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_m
         const int r0 = a.sysRow[sys], n = a.sysRow[sys + 1] - r0;
         const int e0 = a.rowptr[r0];
         float* P = n <= a.smemRows ? pS : a.p32Global + r0;
+        // the system's shared column offsets (read after the barrier below)
+        if (SL && kBatchSys32 && threadIdx.x <= kBatchPatMax)
+            sPat[threadIdx.x] = a.sysPat[(size_t)sys * (kBatchPatMax + 1) + threadIdx.x];
         const int* rp = a.rowptr + r0;
         const int* cl = a.col + e0;
         const double* vl = a.val + e0;
@@ -690,13 +706,14 @@ __global__ void __launch_bounds__(NT, (1536 / NT) > 0 ? 1536 / NT : 1) batched_m
             float pAp = 0.f;
             if (SL) {
                 const int* so = a.sliceOff + a.sliceBase[sys];
+                const int sysL = kBatchSys32 ? sPat[0] : 0;
                 int j = tid >> 5;
                 for (; 32 * (j + NT / 32) < n; j += 2 * (NT / 32)) {
                     float acc0, acc1;
-                    slice_dot2<float, float, 0, kBatchPat32>(so, a.patLen + a.sliceBase[sys],
-                                                                     a.patOff + (size_t)a.sliceBase[sys] * kBatchPatMax,
-                                                                     j, j + NT / 32, a.sval32, a.scol, P, tid & 31,
-                                                                     acc0, acc1);
+                    slice_pair<float, float, 0, kBatchPat32, kBatchSys32>(
+                        so, a.patLen + a.sliceBase[sys], a.patOff + (size_t)a.sliceBase[sys] * kBatchPatMax,
+                        a.meta + a.sliceBase[sys], sPat, sysL, j, j + NT / 32, NT, a.sval32, a.scol, P, tid & 31, acc0,
+                        acc1);
                     const int row0 = 32 * j + (tid & 31), row1 = row0 + NT;
                     if (row0 < n) {
                         Ap[row0] = acc0;
