@@ -202,6 +202,56 @@ __device__ __forceinline__ void st2_policy(double2* p, double2 v, uint64_t pol) 
 // made by fin are visible to every CTA after the barrier.  A wait longer
 // than budgetNs of %globaltimer gives up and returns false.  count must be 0
 // before the launch; partials holds NV * gridDim.x doubles.
+// The same, with the last CTA's thread 0 calling after() once it has released
+// the others: work that no other CTA waits for (a record, a graph condition)
+// then stays off the barrier's critical path.
+template <int NT, int NV, typename Fin, typename After>
+__device__ __forceinline__ bool grid_sum_barrier(const double (&blockTotal)[NV], double* partials, uint32_t* count,
+                                                 uint32_t* gen, Fin fin, After after, uint64_t budgetNs) {
+    __shared__ bool amLast, ok;
+    __shared__ uint32_t genSeen;
+    const int nb = gridDim.x;
+    if (threadIdx.x == 0) {
+        ok = true;
+        genSeen = *(volatile uint32_t*)gen;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) partials[i * nb + blockIdx.x] = blockTotal[i];
+        __threadfence();
+        amLast = atomicAdd(count, 1u) == (uint32_t)nb - 1u;
+    }
+    __syncthreads();
+    if (amLast) {
+        __threadfence();
+        double s[NV];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double a = 0.0;
+            for (int b = threadIdx.x; b < nb; b += NT) a += __ldcg(&partials[i * nb + b]);
+            s[i] = a;
+        }
+        block_sum<NT, NV, double>(s);
+        if (threadIdx.x == 0) {
+            fin(s);
+            *(volatile uint32_t*)count = 0u;
+            __threadfence();
+            atomicAdd(gen, 1u);
+            after();
+        }
+    } else if (threadIdx.x == 0) {
+        const uint64_t t0 = globaltimer_ns();
+        while (*(volatile uint32_t*)gen == genSeen) {
+            if (globaltimer_ns() - t0 > budgetNs) {
+                ok = false;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok;
+}
+
 template <int NT, int NV, typename Fin>
 __device__ __forceinline__ bool grid_sum_barrier(const double (&blockTotal)[NV], double* partials, uint32_t* count,
                                                  uint32_t* gen, Fin fin, uint64_t budgetNs) {
