@@ -995,7 +995,7 @@ __device__ __forceinline__ int system_of_slice(const int* __restrict__ sliceBase
 __global__ void bsell_width_kernel(int nsys, int nslices, const int* __restrict__ sysRow,
                                    const int* __restrict__ sliceBase, const int* __restrict__ rowptr,
                                    const int* __restrict__ col, int* __restrict__ len, int* __restrict__ patLen,
-                                   int* __restrict__ patOff) {
+                                   int* __restrict__ patOff, bool patterns) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nslices; g += warps) {
@@ -1006,7 +1006,7 @@ __global__ void bsell_width_kernel(int nsys, int nslices, const int* __restrict_
         const bool in = lr < n;
         const int j0 = in ? rowptr[r0 + lr] : 0, j1 = in ? rowptr[r0 + lr + 1] : 0;
         const int w = warp_max_i(j1 - j0);
-        bool ok = __all_sync(0xffffffffu, in);
+        bool ok = patterns && __all_sync(0xffffffffu, in);
         int L = 0, q = j0, myOff = 0;
         int cur = q < j1 ? col[q] - lr : INT_MAX;
         while (ok) {
@@ -1111,9 +1111,10 @@ cudaError_t batch_sell_meta(cudaStream_t st, int nsys, int nslices, const int* s
 
 cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
                               const int* rowptr, const int* col, int* sliceLen, int* sliceOff, int* blockSums,
-                              int* patLen, int* patOff) {
+                              int* patLen, int* patOff, bool patterns) {
     const int grid = std::max(1, std::min((nslices * 32 + 255) / 256, device_sm_count() * 32));
-    bsell_width_kernel<<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, col, sliceLen, patLen, patOff);
+    bsell_width_kernel<<<grid, 256, 0, st>>>(nsys, nslices, sysRow, sliceBase, rowptr, col, sliceLen, patLen, patOff,
+                                             patterns);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return scan_exclusive(st, sliceLen, sliceOff, nslices + 1, blockSums);

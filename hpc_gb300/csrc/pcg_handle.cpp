@@ -1728,7 +1728,8 @@ uint32_t PcgHandle::batchSolve(uint32_t nsys, const int32_t* sysRow, const int32
         check(cudaMemsetAsync(m_bsLen.p, 0, sizeof(int32_t) * ((size_t)nsl + 1), m_stream), "memset");
         check(batch_sell_widths(m_stream, (int)nsys, nsl, m_bSysRow.as<int>(), m_bsBase.as<int>(),
                                 m_bRowptr.as<int>(), m_bCol.as<int>(), m_bsLen.as<int>(), m_bsOff.as<int>(),
-                                m_bsScan.as<int>(), m_bsPatLen.as<int>(), m_bsPatOff.as<int>()),
+                                m_bsScan.as<int>(), m_bsPatLen.as<int>(), m_bsPatOff.as<int>(),
+                                envInt("XJPCG_BATCH_PATTERNS", 1) != 0),
               "batch slices");
         alloc(m_bsMeta, sizeof(int32_t) * 2 * ((size_t)nsl + 1), "batch slice records");
         alloc(m_bsSysPat, sizeof(int32_t) * (size_t)(kBatchPatMax + 1) * (nsys + 1), "batch system offsets");

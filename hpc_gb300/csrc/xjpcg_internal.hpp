@@ -226,7 +226,7 @@ cudaError_t batch_sell_meta(cudaStream_t st, int nsys, int nslices, const int* s
                             const int* sliceOff, const int* patLen, const int* patOff, int2* meta, int* sysPat);
 cudaError_t batch_sell_widths(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
                               const int* rowptr, const int* col, int* sliceLen, int* sliceOff, int* blockSums,
-                              int* patLen, int* patOff);
+                              int* patLen, int* patOff, bool patterns);
 template <typename VT>
 cudaError_t batch_sell_fill(cudaStream_t st, int nsys, int nslices, const int* sysRow, const int* sliceBase,
                             const int* rowptr, const int* col, const double* val, const int* sliceOff,

@@ -135,3 +135,25 @@ def test_batched_sliced_irregular_slices(handle, precision, monkeypatch):
             if precision == 0:
                 assert abs(int(r["iters"]) - ref["iters"]) <= max(1, int(0.01 * ref["iters"])), (cfg, s.name)
                 assert np.linalg.norm(x - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"]), (cfg, s.name)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_shared_offsets_same_bits(handle, precision, monkeypatch):
+    # slices whose rows share column offsets store them once; every row then
+    # sums the same products in the same order, with exact zeros between
+    # them, so the solutions equal those of the per-entry layout bit for bit
+    sub = W.batched_stencils(count=24, lo=200, hi=6000, seed=9) + _irregular_batch()
+    # the sliced 512-thread shape with p in shared memory for every system (7),
+    # and with p in global memory for the systems above 4,096 rows (16)
+    for cfg in ("7", "16"):
+        monkeypatch.setenv("XJPCG_BATCH_CFG", cfg)
+        out = {}
+        for pat in ("1", "0"):
+            monkeypatch.setenv("XJPCG_BATCH_PATTERNS", pat)
+            st, xs, res = handle.batch_solve(sub, 20000, 1e-10, precision=precision)
+            assert st == X.SUCCESS, handle.last_message()
+            assert handle.info().batchSliced == 1
+            out[pat] = (xs, res)
+        for a, b in zip(out["1"][0], out["0"][0]):
+            assert np.array_equal(a, b), cfg
+        assert np.array_equal(out["1"][1]["itersRun"], out["0"][1]["itersRun"]), cfg
