@@ -316,11 +316,15 @@ class JPCG:
             raise XJPCGError(st, self.last_message())
         return buf[:cnt.value]
 
-    def adjoint(self, g, diag, max_iter, tol, grad_a=False):
+    def adjoint(self, g, diag, max_iter, tol, grad_a=False, lam=None):
         """lambda = A^-1 g for the last solve's matrix; optionally dL/dA per
-        input entry.  Returns (status, lambda, gradA or None, iters, res)."""
+        input entry.  `lam` (float64, n) receives lambda if given.  Returns
+        (status, lambda, gradA or None, iters, res)."""
         n = len(g)
-        lam = np.zeros(n, np.float64)
+        if lam is None:
+            lam = np.zeros(n, np.float64)
+        elif lam.dtype != np.float64 or lam.size != n or not lam.flags["C_CONTIGUOUS"]:
+            raise ValueError("lam must be a contiguous float64 array of length n")
         ga = np.zeros(self.info().nnz, np.float64) if grad_a else None
         it, res = C.c_uint32(0), C.c_double(0.0)
         st = self.lib.xJPCG_gbAdjointSolve(self.h, _ptr(np.ascontiguousarray(g, np.float64)),
@@ -328,11 +332,16 @@ class JPCG:
                                            max_iter, tol, C.byref(it), C.byref(res), 0)
         return st, lam, ga, it.value, res.value
 
-    def edge_grad(self, ei, ej, c):
+    def edge_grad(self, ei, ej, c, out=None):
+        """dL/dtheta per edge, -c (lambda_i - lambda_j)(x_i - x_j), after an
+        adjoint solve; `out` (float64, one per edge) receives it if given."""
         ei = np.ascontiguousarray(ei, np.int32)
         ej = np.ascontiguousarray(ej, np.int32)
         c = np.ascontiguousarray(c, np.float64)
-        out = np.zeros(ei.size, np.float64)
+        if out is None:
+            out = np.zeros(ei.size, np.float64)
+        elif out.dtype != np.float64 or out.size != ei.size or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float64 array with one entry per edge")
         st = self.lib.xJPCG_gbEdgeGrad(self.h, ei.size, _ptr(ei), _ptr(ej), _ptr(c), _ptr(out), 0)
         if st != SUCCESS:
             raise XJPCGError(st, self.last_message())
