@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
                                                                double* __restrict__ r, double* __restrict__ p,
                                                                double* __restrict__ Apz,
                                                                const double* __restrict__ J, CgState* state,
-                                                               double* partials) {
+                                                               double* partials, int nbSpmv) {
     // Uniform in every CTA: done only changes after the barrier below.
     if (*(volatile uint32_t*)&state->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -236,7 +236,6 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
         }
         return;
     }
-    const double alpha = state->alpha;
     const double rzOld = state->rz;  // the last CTA at the barrier overwrites it
     const uint32_t k0 = state->k;
     const uint64_t keep = l2_policy_evict_last();
@@ -248,11 +247,57 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
     const double2* j2 = reinterpret_cast<const double2*>(J);
     const int stride = gridDim.x * blockDim.x;
     double rr = 0.0, rz = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
-        double2 rv = __ldcs(&r2[i]);
-        const double2 av = __ldcs(&z2[i]), jv = __ldcs(&j2[i]);
-        double2 xv = __ldcs(&x2[i]);
-        const double2 pv = ld2_policy(&p2[i], keep);
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // The first element's loads go out before alpha is known.
+    const bool have0 = i < n2;
+    double2 rv0 = make_double2(0.0, 0.0), av0 = rv0, jv0 = rv0, xv0 = rv0, pv0 = rv0;
+    if (have0) {
+        rv0 = __ldcs(&r2[i]);
+        av0 = __ldcs(&z2[i]);
+        jv0 = __ldcs(&j2[i]);
+        xv0 = __ldcs(&x2[i]);
+        pv0 = ld2_policy(&p2[i], keep);
+    }
+    double alpha;
+    if (nbSpmv > 0) {
+        // alpha = rz / p.Ap from the SpMV's per-CTA partials (kSpmvCgPart), in
+        // the order grid_sum_last<256, 1> adds them, so every CTA forms the
+        // same bits that the SpMV's last CTA would have.
+        __shared__ double sAlpha;
+        double a = 0.0;
+#pragma unroll 4
+        for (int b = threadIdx.x; b < nbSpmv; b += kVecThreads) a += __ldcg(&partials[b]);
+        double s1[1] = {a};
+        block_sum<kVecThreads, 1, double>(s1);
+        if (threadIdx.x == 0) {
+            const double al = rzOld / s1[0];
+            sAlpha = al;
+            if (blockIdx.x == 0) {
+                state->pAp = s1[0];
+                state->alpha = al;
+            }
+        }
+        __syncthreads();
+        alpha = sAlpha;
+    } else {
+        alpha = state->alpha;
+    }
+    double* bar = partials + kFusedPartialOff;  // clear of the SpMV's partials
+    for (bool first = true; i < n2; i += stride, first = false) {
+        double2 rv, av, jv, xv, pv;
+        if (first) {
+            rv = rv0;
+            av = av0;
+            jv = jv0;
+            xv = xv0;
+            pv = pv0;
+        } else {
+            rv = __ldcs(&r2[i]);
+            av = __ldcs(&z2[i]);
+            jv = __ldcs(&j2[i]);
+            xv = __ldcs(&x2[i]);
+            pv = ld2_policy(&p2[i], keep);
+        }
         rv.x = fma(-alpha, av.x, rv.x);
         rv.y = fma(-alpha, av.y, rv.y);
         const double2 zv = make_double2(rv.x * jv.x, rv.y * jv.y);
@@ -302,7 +347,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
         write_record(state, k0, recRr, recRz, alpha, recBeta);
         if (state->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)state->condHandle, recCont ? 1u : 0u);
     };
-    if (!grid_sum_barrier<kVecThreads, 2>(v, partials, &state->counters[3], &state->counters[5], finish, after,
+    if (!grid_sum_barrier<kVecThreads, 2>(v, bar, &state->counters[3], &state->counters[5], finish, after,
                                           kBarrierBudgetNs)) {
         if (threadIdx.x == 0) {
             atomicOr(&state->status, kStatusWaitTimeout);
@@ -313,7 +358,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_fused_kernel(int n4, double* _
     }
     const double beta = __ldcg(&state->fusedBeta);
     if (__ldcg(&state->fusedCont)) {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
+        for (i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
             const double2 zv = ld2_policy(&z2[i], keep);
             double2 pv = ld2_policy(&p2[i], keep);
             pv.x = fma(beta, pv.x, zv.x);
@@ -440,7 +485,7 @@ int fused_grid(int n4, int numSms) {
 }
 
 cudaError_t cg_fused_launch(int grid, cudaStream_t st, int n4, double* x, double* r, double* p, double* Apz,
-                            const double* J, CgState* state, double* partials) {
+                            const double* J, CgState* state, double* partials, int nbSpmv) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(kVecThreads);
@@ -451,7 +496,7 @@ cudaError_t cg_fused_launch(int grid, cudaStream_t st, int n4, double* x, double
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, cg_fused_kernel, n4, x, r, p, Apz, J, state, partials);
+    return cudaLaunchKernelEx(&cfg, cg_fused_kernel, n4, x, r, p, Apz, J, state, partials, nbSpmv);
 }
 
 cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, double* p, const double* z,

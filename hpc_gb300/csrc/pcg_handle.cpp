@@ -980,7 +980,7 @@ void PcgHandle::buildGraph() {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     check(cudaStreamBeginCaptureToGraph(m_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
           "capture body");
-    check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part, kSpmvCgDot,
+    check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part, cgSpmvMode(),
                               &st->done),
           "SpMV kernel");
     iterationTail(n4, st, part);
@@ -990,13 +990,24 @@ void PcgHandle::buildGraph() {
     m_execGen = m_generation;
 }
 
+// The SpMV mode of the fp64 loop.  With the fused vector kernel and a sliced
+// layout (256-thread CTAs), the SpMV only stores its per-CTA partials of p.Ap
+// and the fused kernel forms alpha from them while its first loads are in
+// flight; otherwise the SpMV's last CTA forms alpha.
+int PcgHandle::cgSpmvMode() const {
+    const bool sliced = isSell(m_spmvCfg) || isPat(m_spmvCfg) || isSorted(m_spmvCfg);
+    return (m_fusedUpdate && sliced && m_spmvGrid > 0 && m_spmvGrid <= kFusedPartialOff) ? kSpmvCgPart
+                                                                                         : kSpmvCgDot;
+}
+
 // The vector part of an fp64 iteration after the SpMV: the fused cooperative
 // kernel (update and p update in one launch), or the two separate kernels
 // when XJPCG_FUSED_UPDATE=0.
 void PcgHandle::iterationTail(int n4, CgState* st, double* part) {
     if (m_fusedUpdate) {
         check(cg_fused_launch(fused_grid(n4, m_numSms), m_stream, n4, m_x.as<double>(), m_r.as<double>(),
-                              m_p.as<double>(), m_Ap.as<double>(), m_J.as<double>(), st, part),
+                              m_p.as<double>(), m_Ap.as<double>(), m_J.as<double>(), st, part,
+                              cgSpmvMode() == kSpmvCgPart ? m_spmvGrid : 0),
               "fused update kernel");
         return;
     }
@@ -1047,7 +1058,7 @@ Results PcgHandle::run(uint32_t maxIter, double tol) {
         for (;;) {
             for (int u = 0; u < 16; ++u) {
                 check(spmv64(m_spmvCfg, m_spmvGrid, m_p.as<double>(), m_Ap.as<double>(), nullptr, st, part,
-                                          kSpmvCgDot, &st->done),
+                                          cgSpmvMode(), &st->done),
                       "SpMV kernel");
                 iterationTail(n4, st, part);
             }

@@ -206,6 +206,7 @@ class PcgHandle {
                        int mode, const uint32_t* done);
     void ensureVectors(uint32_t n);
     void buildGraph();
+    int cgSpmvMode() const;
     void iterationTail(int n4, CgState* st, double* part);
     void buildMixedGraph();
     Results readResults(uint32_t maxIter);

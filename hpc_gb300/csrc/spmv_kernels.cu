@@ -37,6 +37,8 @@
 //              krnl_storeApk.cpp:63-73) in one launch.
 //   kResidual  y = b - A x and ||y||^2 reduced into state->rrTrue (true
 //              residual of the mixed-precision refinement loop).
+//   kCgPart    y = A p, and each CTA's partial p.y in partials[blockIdx.x]
+//              (sliced kernel only): the fused vector kernel adds them.
 #include <algorithm>
 #include <cstdio>
 
@@ -45,7 +47,7 @@
 
 namespace xjpcg {
 
-enum SpmvMode : int { kPlain = 0, kCgDot = 1, kResidual = 2 };
+enum SpmvMode : int { kPlain = 0, kCgDot = 1, kResidual = 2, kCgPart = 3 };
 
 template <typename VT>
 struct AccOf {
@@ -478,7 +480,7 @@ __global__ void __launch_bounds__(kSellThreads, SellMinBlocks<VT, U>::value) spm
                 dacc = fma(rv, rv, dacc);
             } else {
                 y[row] = (VT)acc;
-                if (mode == kCgDot) dacc = fma((AccT)x[row], acc, dacc);
+                if (mode == kCgDot || mode == kCgPart) dacc = fma((AccT)x[row], acc, dacc);
             }
         }
     }
@@ -486,6 +488,10 @@ __global__ void __launch_bounds__(kSellThreads, SellMinBlocks<VT, U>::value) spm
     AccT v[1] = {dacc};
     block_sum<kSellThreads, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
+    if (mode == kCgPart) {
+        if (threadIdx.x == 0) partials[blockIdx.x] = tot[0];
+        return;
+    }
     if (grid_sum_last<kSellThreads, 1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
             if (mode == kCgDot) {

@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(kPatThreads, 6) spmv_sellpat_kernel(
                 dacc = fma(rv, rv, dacc);
             } else {
                 y[row] = (VT)acc;
-                if (mode == kSpmvCgDot) dacc = fma((AccT)x[row], acc, dacc);
+                if (mode == kSpmvCgDot || mode == kSpmvCgPart) dacc = fma((AccT)x[row], acc, dacc);
             }
         }
     }
@@ -299,6 +299,10 @@ __global__ void __launch_bounds__(kPatThreads, 6) spmv_sellpat_kernel(
     AccT v[1] = {dacc};
     block_sum<kPatThreads, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
+    if (mode == kSpmvCgPart) {
+        if (threadIdx.x == 0) partials[blockIdx.x] = tot[0];
+        return;
+    }
     if (grid_sum_last<kPatThreads, 1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
             if (mode == kSpmvCgDot) {
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(kPatThreads, 3) spmv_sellpat_tma_kernel(
                 dacc = fma(rv, rv, dacc);
             } else {
                 y[row] = (VT)acc;
-                if (mode == kSpmvCgDot) dacc = fma((AccT)x[row], acc, dacc);
+                if (mode == kSpmvCgDot || mode == kSpmvCgPart) dacc = fma((AccT)x[row], acc, dacc);
             }
         }
         __syncwarp();  // every lane is done with cur before it is refilled
@@ -445,6 +449,10 @@ __global__ void __launch_bounds__(kPatThreads, 3) spmv_sellpat_tma_kernel(
     AccT v[1] = {dacc};
     block_sum<kPatThreads, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
+    if (mode == kSpmvCgPart) {
+        if (threadIdx.x == 0) partials[blockIdx.x] = tot[0];
+        return;
+    }
     if (grid_sum_last<kPatThreads, 1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
             if (mode == kSpmvCgDot) {

@@ -192,13 +192,17 @@ __global__ void __launch_bounds__(kSortThreads) spmv_sellsort_kernel(
             dacc = fma(rv, rv, dacc);
         } else {
             y[row] = (VT)acc;
-            if (mode == kSpmvCgDot) dacc = fma((AccT)x[row], acc, dacc);
+            if (mode == kSpmvCgDot || mode == kSpmvCgPart) dacc = fma((AccT)x[row], acc, dacc);
         }
     }
     if (mode == kSpmvPlain) return;
     AccT v[1] = {dacc};
     block_sum<kSortThreads, 1, AccT>(v);
     double tot[1] = {(double)v[0]}, fin[1];
+    if (mode == kSpmvCgPart) {
+        if (threadIdx.x == 0) partials[blockIdx.x] = tot[0];
+        return;
+    }
     if (grid_sum_last<kSortThreads, 1>(tot, partials, &state->counters[0], fin)) {
         if (threadIdx.x == 0) {
             if (mode == kSpmvCgDot) {

@@ -42,7 +42,10 @@ template <typename VT>
 cudaError_t spmv_launch(int cfg, int grid, cudaStream_t st, int n, const int* rowptr, const int* col, const VT* val,
                         const VT* x, VT* y, const VT* b, CgState* state, double* partials, int mode,
                         const uint32_t* doneFlag);
-enum : int { kSpmvPlain = 0, kSpmvCgDot = 1, kSpmvResidual = 2 };
+// kSpmvCgPart: y = A p and each CTA's partial p.y in partials[blockIdx.x],
+// with no grid reduction: the fused vector kernel adds them (kernels with
+// 256-thread CTAs, whose order it repeats; spmv_config_partials says which).
+enum : int { kSpmvPlain = 0, kSpmvCgDot = 1, kSpmvResidual = 2, kSpmvCgPart = 3 };
 
 // ---- sliced SpMV layout (spmv_kernels.cu) ----
 int sell_num_configs();
@@ -147,8 +150,12 @@ int update_grid(int n4, int numSms);
 // update + p update in one cooperative launch (cg_kernels.cu); grid from
 // fused_grid (every CTA resident); partials hold 2 * grid doubles.
 int fused_grid(int n4, int numSms);
+// The fused kernel's barrier uses partials[kFusedPartialOff ...), clear of an
+// SpMV's per-CTA partials (at most kFusedPartialOff CTAs); nbSpmv > 0: alpha
+// from the SpMV's kSpmvCgPart partials, 0: alpha from the state.
+constexpr int kFusedPartialOff = 8192;
 cudaError_t cg_fused_launch(int grid, cudaStream_t st, int n4, double* x, double* r, double* p, double* Apz,
-                            const double* J, CgState* state, double* partials);
+                            const double* J, CgState* state, double* partials, int nbSpmv);
 cudaError_t cg_init_launch(int grid, cudaStream_t st, int n, int n4, const double* b, const double* diag, double* x,
                            double* r, double* p, double* J, double* Ap, CgState* state, double* partials);
 // update: r -= alpha Ap, then z = J r is written over Ap; p update reads it
