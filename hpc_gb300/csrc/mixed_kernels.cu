@@ -18,14 +18,20 @@
 // One CUDA graph per matrix:
 //   rel_init                        x = 0, d = 0, J = 1/diag, r = b, p = J r
 //   WHILE not done:
-//     SpMV fp32, kCgDot             Ap = A p, p.Ap, alpha
-//     rel_update                    d += alpha p, r -= alpha Ap, r.r, r.z,
-//                                   beta; decides the refresh (IF condition)
-//     IF refresh:
-//       rel_fold                    x += d (FP64), d = 0
-//       SpMV fp64, kResidual        r64 = b - A x, ||r64||^2
-//       rel_restart                 r = r64, r.z, beta, stop test
+//     WHILE no refresh is due:
+//       SpMV fp32, kCgDot           Ap = A p, p.Ap, alpha
+//       rel_update                  d += alpha p, r -= alpha Ap, r.r, r.z,
+//                                   beta; decides the refresh (ends the
+//                                   inner loop)
+//       rel_pupdate                 p = J r + beta p (skipped when a
+//                                   refresh is due)
+//     rel_fold                      x += d (FP64), d = 0
+//     SpMV fp64, kResidual          r64 = b - A x, ||r64||^2
+//     rel_restart                   r = r64, r.z, beta, stop test; clears
+//                                   the refresh flag, re-arms the inner loop
 //     rel_pupdate                   p = J r + beta p
+// The refresh runs a few times per solve, so the FP32 iterations carry no
+// conditional node of their own.
 // Without graphs (XJPCG_HOST_LOOP=1, for profilers) the host launches the six
 // kernels of every iteration in batches; the refresh kernels then return at
 // once unless the update kernel chose a refresh (reliable / skipRefresh),
@@ -181,7 +187,7 @@ __global__ void __launch_bounds__(kMxThreads, 5) rel_update_kernel(int n4, float
             st->beta = rzN / st->rz;
             st->rz = rzN;
         }
-        if (st->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)st->relHandle, refresh ? 1u : 0u);
+        if (st->useCond) cudaGraphSetConditional((cudaGraphConditionalHandle)st->relHandle, refresh ? 0u : 1u);
     }
 }
 
@@ -224,14 +230,19 @@ __global__ void __launch_bounds__(kMxThreads) rel_restart_kernel(int n4, const d
         }
         st->done = stop ? 1u : 0u;
         if (stop) st->skipRefresh = 1u;
-        if (st->useCond && stop) cudaGraphSetConditional((cudaGraphConditionalHandle)st->condHandle, 0u);
+        st->reliable = 0u;  // the refresh is done: the next p update runs
+        if (st->useCond) {
+            if (stop) cudaGraphSetConditional((cudaGraphConditionalHandle)st->condHandle, 0u);
+            cudaGraphSetConditional((cudaGraphConditionalHandle)st->relHandle, stop ? 0u : 1u);
+        }
     }
 }
 
 __global__ void __launch_bounds__(kMxThreads) rel_pupdate_kernel(int n4, float* __restrict__ p,
                                                                  const float* __restrict__ r,
                                                                  const float* __restrict__ J, CgState* st) {
-    if (*(volatile uint32_t*)&st->done) return;
+    // A due refresh changes r and beta first; the p update after it runs then.
+    if (*(volatile uint32_t*)&st->done || *(volatile uint32_t*)&st->reliable) return;
     const float beta = (float)st->beta;
     const int n4q = n4 >> 2;
     float4* p4 = reinterpret_cast<float4*>(p);

@@ -1135,35 +1135,28 @@ void PcgHandle::buildMixedGraph() {
     cudaGraphNode_t loopNode;
     check(cudaGraphAddNode(&loopNode, g, nodes.data(), nullptr, nn, &cp), "loop node");
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    // body: FP32 SpMV + update, then IF refresh, then p update
-    check(cudaGraphConditionalHandleCreate(&m_condInner, body, 0, 0), "handle");
-    check(cudaStreamBeginCaptureToGraph(m_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+    // body: WHILE no refresh is due {FP32 SpMV, update, p update}, then the
+    // refresh (fold, FP64 residual, restart) and its p update
+    check(cudaGraphConditionalHandleCreate(&m_condInner, body, 1, cudaGraphCondAssignDefault), "handle");
+    cudaGraphNodeParams ip = {};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = m_condInner;
+    ip.conditional.type = cudaGraphCondTypeWhile;
+    ip.conditional.size = 1;
+    cudaGraphNode_t innerNode;
+    check(cudaGraphAddNode(&innerNode, body, nullptr, nullptr, 0, &ip), "inner loop node");
+    cudaGraph_t inner = ip.conditional.phGraph_out[0];
+    check(cudaStreamBeginCaptureToGraph(m_stream, inner, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
           "capture");
     check(spmv32(cfg32, grid32, m_p32.as<float>(), m_Ap32.as<float>(), nullptr, st, part, kSpmvCgDot, &st->done),
           "SpMV fp32");
     check(rel_update_launch(update_grid(n4, m_numSms), m_stream, n4, m_d32.as<float>(), m_r32.as<float>(), m_p32.as<float>(),
                             m_Ap32.as<float>(), m_J32.as<float>(), st, part),
           "mixed update");
-    check(cudaStreamEndCapture(m_stream, &body), "capture end");
-    size_t bn = 0;
-    check(cudaGraphGetNodes(body, nullptr, &bn), "nodes");
-    std::vector<cudaGraphNode_t> bnodes(bn);
-    check(cudaGraphGetNodes(body, bnodes.data(), &bn), "nodes");
-    std::vector<cudaGraphNode_t> leaves;
-    for (auto nd : bnodes) {
-        size_t cnt = 0;
-        check(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &cnt), "deps");
-        if (cnt == 0) leaves.push_back(nd);
-    }
-    cudaGraphNodeParams ip = {};
-    ip.type = cudaGraphNodeTypeConditional;
-    ip.conditional.handle = m_condInner;
-    ip.conditional.type = cudaGraphCondTypeIf;
-    ip.conditional.size = 1;
-    cudaGraphNode_t ifNode;
-    check(cudaGraphAddNode(&ifNode, body, leaves.data(), nullptr, leaves.size(), &ip), "refresh node");
-    cudaGraph_t refresh = ip.conditional.phGraph_out[0];
-    check(cudaStreamBeginCaptureToGraph(m_stream, refresh, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+    check(rel_pupdate_launch(vg, m_stream, n4, m_p32.as<float>(), m_r32.as<float>(), m_J32.as<float>(), st),
+          "p fp32");
+    check(cudaStreamEndCapture(m_stream, &inner), "capture end");
+    check(cudaStreamBeginCaptureToGraph(m_stream, body, &innerNode, nullptr, 1, cudaStreamCaptureModeThreadLocal),
           "capture");
     check(rel_fold_launch(vg, m_stream, n4, m_x.as<double>(), m_d32.as<float>(), st), "fold");
     check(spmv64(m_spmvCfg, m_spmvGrid, m_x.as<double>(), m_r.as<double>(), m_b.as<double>(), st, part,
@@ -1171,9 +1164,6 @@ void PcgHandle::buildMixedGraph() {
           "residual SpMV");
     check(rel_restart_launch(vg, m_stream, n4, m_r.as<double>(), m_J32.as<float>(), m_r32.as<float>(), st, part),
           "restart");
-    check(cudaStreamEndCapture(m_stream, &refresh), "capture end");
-    check(cudaStreamBeginCaptureToGraph(m_stream, body, &ifNode, nullptr, 1, cudaStreamCaptureModeThreadLocal),
-          "capture");
     check(rel_pupdate_launch(vg, m_stream, n4, m_p32.as<float>(), m_r32.as<float>(), m_J32.as<float>(), st),
           "p fp32");
     check(cudaStreamEndCapture(m_stream, &body), "capture end");

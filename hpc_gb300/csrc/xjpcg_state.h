@@ -45,7 +45,7 @@ struct alignas(16) CgState {
     uint32_t reliable;             // mixed precision: this iteration refreshes the residual
     double rrMax;                  // mixed precision: largest r.r since the last refresh
     double delta2;                 // mixed precision: refresh when r.r < delta2 * rrMax
-    uint64_t relHandle;            // mixed precision: conditional handle of the refresh
+    uint64_t relHandle;            // mixed precision: conditional handle of the inner FP32 loop (0: a refresh is due)
     uint32_t skipRefresh;          // mixed precision: 1 = the refresh kernels of this iteration return at once
     uint32_t xSkip;                // fp64: 1 = the update kernel found the loop done (no x update due)
     uint32_t pupdateDue;           // reference-order loop: 1 = this iteration's p update is due
