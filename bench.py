@@ -613,7 +613,11 @@ def run_gb300(args):
     ttt = t / args.steps
     value = replicas_value(world, args.steps, t)
     k_iters = int(np.median(iters))
-    launches = sum(1 + 3 * k for k in iters)
+    # per solve: the init kernel, then whole passes of the loop body (kernels
+    # past the stop in the last pass launch and return at once)
+    inf_l = h.info()
+    per_pass = inf_l.kernelsPerIter * inf_l.loopUnroll
+    launches = sum(1 + per_pass * -(-k // inf_l.loopUnroll) for k in iters)
 
     # Dominant kernel: the SpMV, timed alone on the same stream and matrix.
     spmv_ms = None

@@ -60,7 +60,8 @@ class GbInfo(C.Structure):
                 ("batchSmemRows", C.c_uint32), ("batchGrid", C.c_uint32), ("batchMs", C.c_double),
                 ("spmvCfg", C.c_uint32), ("spmvCfg32", C.c_uint32), ("spmvLayout32", C.c_uint32),
                 ("batchSliced", C.c_uint32), ("tuneMs", C.c_double), ("uploadMs", C.c_double),
-                ("uploadIdxMs", C.c_double), ("uploadValMs", C.c_double)]
+                ("uploadIdxMs", C.c_double), ("uploadValMs", C.c_double), ("loopUnroll", C.c_uint32),
+                ("kernelsPerIter", C.c_uint32)]
 
 
 class GbSignature(C.Structure):

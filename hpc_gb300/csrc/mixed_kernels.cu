@@ -97,6 +97,9 @@ __global__ void __launch_bounds__(kMxThreads, 5) rel_update_kernel(int n4, float
         }
         return;
     }
+    // A refresh is due (an earlier copy of this kernel in the same pass of
+    // the inner loop chose it): nothing to do until the refresh has run.
+    if (*(volatile uint32_t*)&st->reliable) return;
     const double alphaD = st->alpha;
     const float alpha = (float)alphaD;
     float rr = 0.f, rz = 0.f;

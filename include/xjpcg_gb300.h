@@ -49,6 +49,8 @@ typedef struct {
     double uploadMs;       /* device time of the last COO matrix upload (H2D, part of m_matProc) */
     double uploadIdxMs;    /* of which the row and column index copies (on the handle's stream) */
     double uploadValMs;    /* of which the value copy (on the side stream, from its start) */
+    uint32_t loopUnroll;   /* iterations per pass of a graph loop's body (kernels past the stop return at once) */
+    uint32_t kernelsPerIter; /* kernels per fp64 iteration: 2 (SpMV, fused vector kernel) or 3 (separate) */
 } XJPCG_GbInfo_t;
 
 /* Per-system outcome of a batched solve. */
