@@ -207,6 +207,7 @@ class PcgHandle {
     void ensureVectors(uint32_t n);
     void buildGraph();
     int cgSpmvMode() const;
+    void mixedUpdate(int n4, int vg, CgState* st, double* part, bool pUpdate = true);
     void iterationTail(int n4, CgState* st, double* part);
     void buildMixedGraph();
     Results readResults(uint32_t maxIter);

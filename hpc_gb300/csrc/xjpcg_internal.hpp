@@ -167,6 +167,9 @@ cudaError_t cg_pupdate_launch(int grid, cudaStream_t st, int n4, double* x, doub
 // ---- mixed precision, reliable updates (mixed_kernels.cu) ----
 cudaError_t rel_init_launch(int grid, cudaStream_t s, int n, int n4, const double* b, const double* diag, double* x,
                             float* d, float* J, float* r, float* p, CgState* st, double* partials);
+int rel_fused_grid(int n4, int numSms);
+cudaError_t rel_fused_launch(int grid, cudaStream_t s, int n4, float* d, float* r, float* p, const float* Ap,
+                             const float* J, CgState* st, double* partials);
 cudaError_t rel_update_launch(int grid, cudaStream_t s, int n4, float* d, float* r, const float* p, const float* Ap,
                               const float* J, CgState* st, double* partials);
 cudaError_t rel_fold_launch(int grid, cudaStream_t s, int n4, double* x, float* d, const CgState* st);

@@ -51,6 +51,7 @@ struct alignas(16) CgState {
     uint32_t pupdateDue;           // reference-order loop: 1 = this iteration's p update is due
     uint32_t fusedCont;            // fused update: 1 = the loop goes on (the p update is due)
     double fusedBeta;              // fused update: beta, published at its grid barrier
+    uint32_t pDone;                // mixed precision: 1 = the fused update already updated p this iteration
 };
 
 }  // namespace xjpcg
