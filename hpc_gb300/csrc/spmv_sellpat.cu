@@ -192,24 +192,6 @@ __global__ void sp_fill_kernel(int n, const int* __restrict__ rowptr, const int*
 }
 
 
-// Streaming value load (evict-first) that asks L2 to fetch the whole 256-byte
-// block: a warp reads a slice's columns in order, 128 B (FP32) or 256 B
-// (FP64) each, so the next column's line is the neighbour.  The 160^3 mixed
-// solve took 74.4 ms with it against 74.8 ms with plain streaming loads.
-template <typename T>
-__device__ __forceinline__ T ld_val(const T* p) {
-    T v;
-    if (sizeof(T) == 8) {
-        double d;
-        asm("ld.global.cs.L2::256B.f64 %0, [%1];" : "=d"(d) : "l"(p));
-        v = (T)d;
-    } else {
-        float f;
-        asm("ld.global.cs.L2::256B.f32 %0, [%1];" : "=f"(f) : "l"(p));
-        v = (T)f;
-    }
-    return v;
-}
 template <typename VT, int U, bool RUNS>
 __global__ void __launch_bounds__(kPatThreads, 6) spmv_sellpat_kernel(
     int n, int nslices, const int* __restrict__ sliceOff, const int* __restrict__ patLen,
