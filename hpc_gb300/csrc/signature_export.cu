@@ -486,9 +486,12 @@ __global__ void __launch_bounds__(1024) sig_chan_scan_kernel(int P, const long l
     }
 }
 
-// One thread per 4-slot group: its value word and, at the chunk's index
-// positions, the row-index and column-index words.
-__global__ void sig_format_kernel(int nGroups, int P, const int* __restrict__ ppad, const int* __restrict__ chStart,
+// One warp per chunk (partition p, channel c; idx = p kCh + c), its lanes
+// taking the chunk's 4-slot groups g = lane, lane + 32, ...: each group's
+// value word and, at the chunk's index positions, the row-index and
+// column-index words.  A warp reads its chunk's place in the channel stream
+// once; no group searches for its partition or channel.
+__global__ void sig_format_kernel(int P, const int* __restrict__ ppad, const int* __restrict__ chStart,
                                   const int* __restrict__ chLen, const int* __restrict__ chMinG,
                                   const int* __restrict__ partBlock, const int* __restrict__ blkRow0,
                                   const long long* __restrict__ chOff, const long long* __restrict__ chanBase,
@@ -501,66 +504,66 @@ __global__ void sig_format_kernel(int nGroups, int P, const int* __restrict__ pp
         h[0] = make_uint4(hd[0], hd[1], hd[2], hd[3]);
         h[1] = make_uint4(0u, 0u, 0u, 0u);
     }
-    for (int G = blockIdx.x * blockDim.x + threadIdx.x; G < nGroups; G += gridDim.x * blockDim.x) {
-        const int slot = G * kPar;
-        const int p = upper_index(ppad, P + 1, slot) - 1;
-        const int rel = slot - ppad[p];
-        int c = 0;
-        while (c < kCh - 1 && !(rel >= chStart[p * kCh + c] && rel < chStart[p * kCh + c] + chLen[p * kCh + c])) ++c;
-        const int idx = p * kCh + c;
-        const int i = rel - chStart[idx];
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < P * kCh; idx += warps) {
         const int len = chLen[idx];
-        const int g = i / kPar;
+        if (len <= 0) continue;
+        const int p = idx / kCh, c = idx % kCh;
         const int abs0 = ppad[p] + chStart[idx];
         unsigned char* cb = out + chanBase[c] + 32 + chOff[(size_t)c * P + p];
-        double v[kPar];
+        const int r0 = blkRow0[partBlock[p]];
+        const int g0 = chMinG[idx];
+        for (int i = lane * kPar; i < len; i += 32 * kPar) {
+            const int slot = abs0 + i;
+            const int g = i / kPar;
+            double v[kPar];
 #pragma unroll
-        for (int k = 0; k < kPar; ++k) {
-            const uint32_t s = slotSrc[slot + k];
-            v[k] = s == kPadSrc ? 0.0 : val[s];
-        }
-        double2* vd = reinterpret_cast<double2*>(cb + 32ll * (g + g / 128 + g / 16 + 2));
-        vd[0] = make_double2(v[0], v[1]);
-        vd[1] = make_double2(v[2], v[3]);
-        if (g % 128 == 0) {
-            const int r0 = blkRow0[partBlock[p]];
-            uint32_t w[8];
-            for (int k = 0; k < 16; k += 2) {
-                uint32_t h2[2];
-                for (int t = 0; t < 2; ++t) {
-                    const int pos = i + (k + t) * kRowSlots;
-                    int r = 0;
-                    if (pos < len)
-                        r = grpRow[(abs0 + pos) >> 2] - r0;
-                    else if (i >= kRowWordSlots)
-                        r = grpRow[(abs0 + pos - kRowWordSlots) >> 2] - r0;
-                    h2[t] = (uint32_t)(uint16_t)r;
-                }
-                w[k / 2] = h2[0] | (h2[1] << 16);
+            for (int k = 0; k < kPar; ++k) {
+                const uint32_t src = slotSrc[slot + k];
+                v[k] = src == kPadSrc ? 0.0 : val[src];
             }
-            uint4* d = reinterpret_cast<uint4*>(cb + 32ll * (g + g / 128 + g / 16));
-            d[0] = make_uint4(w[0], w[1], w[2], w[3]);
-            d[1] = make_uint4(w[4], w[5], w[6], w[7]);
-        }
-        if (g % 16 == 0) {
-            const int g0 = chMinG[idx];
-            uint32_t w[8];
-            for (int k = 0; k < 16; k += 2) {
-                uint32_t h2[2];
-                for (int t = 0; t < 2; ++t) {
-                    const int pos = i + (k + t) * kPar;
-                    int cg = 0;
-                    if (pos < len)
-                        cg = grpG[(abs0 + pos) >> 2] - g0;
-                    else if (i >= kColWordSlots)
-                        cg = grpG[(abs0 + pos - kColWordSlots) >> 2] - g0;
-                    h2[t] = (uint32_t)(uint16_t)cg;
+            double2* vd = reinterpret_cast<double2*>(cb + 32ll * (g + g / 128 + g / 16 + 2));
+            vd[0] = make_double2(v[0], v[1]);
+            vd[1] = make_double2(v[2], v[3]);
+            if (g % 128 == 0) {
+                uint32_t w[8];
+                for (int k = 0; k < 16; k += 2) {
+                    uint32_t h2[2];
+                    for (int t = 0; t < 2; ++t) {
+                        const int pos = i + (k + t) * kRowSlots;
+                        int r = 0;
+                        if (pos < len)
+                            r = grpRow[(abs0 + pos) >> 2] - r0;
+                        else if (i >= kRowWordSlots)
+                            r = grpRow[(abs0 + pos - kRowWordSlots) >> 2] - r0;
+                        h2[t] = (uint32_t)(uint16_t)r;
+                    }
+                    w[k / 2] = h2[0] | (h2[1] << 16);
                 }
-                w[k / 2] = h2[0] | (h2[1] << 16);
+                uint4* d = reinterpret_cast<uint4*>(cb + 32ll * (g + g / 128 + g / 16));
+                d[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                d[1] = make_uint4(w[4], w[5], w[6], w[7]);
             }
-            uint4* d = reinterpret_cast<uint4*>(cb + 32ll * (g + g / 128 + 1 + g / 16));
-            d[0] = make_uint4(w[0], w[1], w[2], w[3]);
-            d[1] = make_uint4(w[4], w[5], w[6], w[7]);
+            if (g % 16 == 0) {
+                uint32_t w[8];
+                for (int k = 0; k < 16; k += 2) {
+                    uint32_t h2[2];
+                    for (int t = 0; t < 2; ++t) {
+                        const int pos = i + (k + t) * kPar;
+                        int cg = 0;
+                        if (pos < len)
+                            cg = grpG[(abs0 + pos) >> 2] - g0;
+                        else if (i >= kColWordSlots)
+                            cg = grpG[(abs0 + pos - kColWordSlots) >> 2] - g0;
+                        h2[t] = (uint32_t)(uint16_t)cg;
+                    }
+                    w[k / 2] = h2[0] | (h2[1] << 16);
+                }
+                uint4* d = reinterpret_cast<uint4*>(cb + 32ll * (g + g / 128 + 1 + g / 16));
+                d[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                d[1] = make_uint4(w[4], w[5], w[6], w[7]);
+            }
         }
     }
 }
@@ -764,9 +767,8 @@ void SigExport::build(cudaStream_t st, uint32_t n, uint64_t nnz64, const int* ro
 }
 
 void SigExport::format(cudaStream_t st, const double* val) {
-    const int groups = (int)(nnzPad / kPar);
-    sig_format_kernel<<<grid_of(std::max(groups, 1), 256), 256, 0, st>>>(
-        groups, P, bPpad.as<int>(), bChStart.as<int>(), bChLen.as<int>(), bChMinG.as<int>(), bPartBlock.as<int>(),
+    sig_format_kernel<<<grid_of((int64_t)P * kCh * 32, 256), 256, 0, st>>>(
+        P, bPpad.as<int>(), bChStart.as<int>(), bChLen.as<int>(), bChMinG.as<int>(), bPartBlock.as<int>(),
         bBlkRow0.as<int>(), bChOff.as<long long>(), bChanBase.as<long long>(), bChanHdr.as<uint32_t>(),
         bSlotSrc.as<uint32_t>(), bGrpRow.as<int>(), bGrpG.as<int>(), val, bOut.as<unsigned char>());
     SIG_CHECK(cudaGetLastError(), "signature values");
