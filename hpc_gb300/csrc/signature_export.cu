@@ -270,24 +270,39 @@ __global__ void sig_part_range_kernel(int P, int nnzPad, const int* __restrict__
         ppad[p] = p == P ? nnzPad : segOff[segBase[p]];
 }
 
-// Second placement pass: source slot of every entry, row and column group of
-// every 4-slot group (trailing padding groups keep the last column group).
+// Second placement pass: source slot of every entry (kPadSrc in the padding
+// slots), row and column group of every 4-slot group (trailing padding groups
+// keep the last column group).  A group's four slots are assembled in
+// registers and stored as one 16-byte word once the group is complete, so
+// every slot is written once and none needs a fill beforehand (segments
+// start on 32-slot boundaries, groups on 4-slot ones).
 __global__ void sig_emit_kernel(int S, const int* __restrict__ segLo, const int* __restrict__ segHi,
                                 const int* __restrict__ col, const int* __restrict__ segOff,
                                 const int* __restrict__ segLen, const int* __restrict__ segRow,
                                 uint32_t* __restrict__ slotSrc, int* __restrict__ grpRow, int* __restrict__ grpG) {
+    const uint4 pad = make_uint4(kPadSrc, kPadSrc, kPadSrc, kPadSrc);
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
         const int off = segOff[s], row = segRow[s];
         Placement pl;
+        uint4 cur = pad;
         for (int j = segLo[s]; j < segHi[s]; ++j) {
             const int c = col[j];
             if (pl.place(c)) {
+                if (pl.gs > 0) *reinterpret_cast<uint4*>(slotSrc + off + pl.gs - kPar) = cur;
+                cur = pad;
                 grpRow[(off + pl.gs) >> 2] = row;
                 grpG[(off + pl.gs) >> 2] = pl.curG;
             }
-            slotSrc[off + pl.gs + (c & 3)] = (uint32_t)j;
+            const uint32_t src = (uint32_t)j;
+            const int m = c & 3;
+            cur.x = m == 0 ? src : cur.x;
+            cur.y = m == 1 ? src : cur.y;
+            cur.z = m == 2 ? src : cur.z;
+            cur.w = m == 3 ? src : cur.w;
         }
+        if (pl.gs >= 0) *reinterpret_cast<uint4*>(slotSrc + off + pl.gs) = cur;
         for (int k = pl.gs + kPar; k < segLen[s]; k += kPar) {
+            *reinterpret_cast<uint4*>(slotSrc + off + k) = pad;
             grpRow[(off + k) >> 2] = row;
             grpG[(off + k) >> 2] = pl.curG;
         }
@@ -715,7 +730,7 @@ void SigExport::build(cudaStream_t st, uint32_t n, uint64_t nnz64, const int* ro
     grow(bSlotSrc, sizeof(uint32_t) * (size_t)nnzPad, "signature slots");
     grow(bGrpRow, sizeof(int) * groups, "signature groups");
     grow(bGrpG, sizeof(int) * groups, "signature groups");
-    SIG_CHECK(cudaMemsetAsync(bSlotSrc.p, 0xff, sizeof(uint32_t) * (size_t)nnzPad, st), "memset");
+    // sig_emit_kernel writes every slot, padding included
     sig_emit_kernel<<<grid_of(S, 256), 256, 0, st>>>(S, bSegLo.as<int>(), bSegHi.as<int>(), col, bSegOff.as<int>(),
                                                       bSegLen.as<int>(), bSegRow.as<int>(), bSlotSrc.as<uint32_t>(),
                                                       bGrpRow.as<int>(), bGrpG.as<int>());
