@@ -428,8 +428,9 @@ cudaError_t rel_init_launch(int grid, cudaStream_t s, int n, int n4, const doubl
     rel_init_kernel<<<grid, kMxThreads, 0, s>>>(n, n4, b, diag, x, d, J, r, p, st, partials);
     return cudaGetLastError();
 }
-// At most the CTAs that fit at once (a cooperative launch), up to five per SM
-// as rel_update_kernel runs, so that the partials add in the same order.
+// At most the CTAs that fit at once (a cooperative launch), capped at three
+// per SM as for the fp64 kernel: fewer CTAs meet at the barrier.  160^3 mixed
+// solve: 74.6 ms with three or two per SM, 75.2 ms with four (the most that fit).
 int rel_fused_grid(int n4, int numSms) {
     int perSm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, rel_fused_kernel, kMxThreads, 0) != cudaSuccess ||
@@ -437,7 +438,7 @@ int rel_fused_grid(int n4, int numSms) {
         cudaGetLastError();
         perSm = 1;
     }
-    perSm = std::min(perSm, 5);
+    perSm = std::min(perSm, 3);
     const int need = std::max(1, (n4 / 4 + kMxThreads - 1) / kMxThreads);
     return std::min(need, numSms * perSm);
 }
