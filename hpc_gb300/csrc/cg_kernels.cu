@@ -475,11 +475,14 @@ int fused_grid(int n4, int numSms) {
         perSm = 1;
     }
     // Three CTAs per SM (768 threads, about 18 elements each on 160^3) measured
-    // best: 0.2699 ms per iteration against 0.2713 - 0.2724 with 4 to 6 and
-    // 0.2779 with 2.  Fewer CTAs shorten the barrier and its partial sums.
-    // With the record written after the release: 0.2688 ms (3) against 0.2702
-    // (4); on the 885k-row 7-point system 45.6 us (3), 44.5 (2), 47.9 (1).
-    perSm = std::min(perSm, 3);
+    // best on 160^3: 0.2699 ms per iteration against 0.2713 - 0.2724 with 4 to
+    // 6 and 0.2779 with 2.  Fewer CTAs shorten the barrier and its partial
+    // sums.  Below about 1.2 M element pairs two CTAs per SM do better (us per
+    // iteration, three against two, with the loop as it is now): 27-point
+    // 160^3 265.6 / 274.8, 140^3 185.6 / 186.0, 128^3 151.0 / 145.4, 100^3
+    // 80.3 / 79.2; the 885k-row 7-point system 42.4 / 41.8.
+    const int n2 = n4 / 2;
+    perSm = std::min(perSm, n2 < 1200000 ? 2 : 3);
     const int need = std::max(1, (n4 / 2 + kVecThreads - 1) / kVecThreads);
     return std::min(need, numSms * perSm);
 }
